@@ -1,0 +1,133 @@
+"""ctypes binding of libanacor_gb300.so.
+
+The library is loaded from the package's in-tree ``_build`` directory.  If it
+is missing the import of the binding raises: there is no host fallback for
+the absorption path.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_i8p = np.ctypeslib.ndpointer(dtype=np.int8, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i8ppp = ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8)))
+
+# every symbol declared in include/anacor_gb300.h
+EXPORTS = (
+    "ray_tracing_overall", "ray_tracing_single", "ib_test", "ray_tracing_gpu_overall",
+    "anacor_last_status", "anacor_last_error", "anacor_version", "anacor_absorption",
+    "anacor_plan_create", "anacor_plan_set_reflections", "anacor_plan_run", "anacor_plan_result",
+    "anacor_plan_device_result", "anacor_plan_n_refl", "anacor_plan_launch_info", "anacor_plan_destroy",
+    "anacor_plan_count_steps",
+    "anacor_batch_run", "anacor_rotated_vectors", "anacor_leg_detail",
+)
+
+_LIB = None
+
+
+class AnacorError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"anacor status {status}: {msg}")
+        self.status = status
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(path: str | None = None) -> ct.CDLL:
+    """Load (once) and type the library.  Raises if it has not been built."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    path = path or _build.LIB
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m anacor_public_gb300.build` "
+                          "(the absorption path has no CPU fallback)")
+    L = ct.CDLL(path)
+    # drop-ins, argtypes as AnACor/utils/utils_mp.py:59-148
+    L.ray_tracing_overall.restype = ct.POINTER(ct.c_double)
+    L.ray_tracing_overall.argtypes = [ct.c_int64, ct.c_int64, np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int64,
+                                      np.ctypeslib.ndpointer(dtype=np.float64),
+                                      np.ctypeslib.ndpointer(dtype=np.float64),
+                                      np.ctypeslib.ndpointer(dtype=np.float64),
+                                      np.ctypeslib.ndpointer(dtype=np.float64),
+                                      np.ctypeslib.ndpointer(dtype=np.float64), ct.c_int64,
+                                      np.ctypeslib.ndpointer(dtype=np.float64),
+                                      np.ctypeslib.ndpointer(dtype=np.float64), _i8ppp,
+                                      np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int, ct.c_int, ct.c_int,
+                                      ct.c_int]
+    L.ray_tracing_single.restype = ct.c_double
+    L.ray_tracing_single.argtypes = [np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int64,
+                                     np.ctypeslib.ndpointer(dtype=np.float64),
+                                     np.ctypeslib.ndpointer(dtype=np.float64),
+                                     np.ctypeslib.ndpointer(dtype=np.float64),
+                                     np.ctypeslib.ndpointer(dtype=np.float64), _i8ppp,
+                                     np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int, ct.c_int64, ct.c_int]
+    L.ib_test.restype = ct.c_double
+    L.ib_test.argtypes = [np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int64,
+                          np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64),
+                          np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64),
+                          _i8ppp, np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int, ct.c_int64, ct.c_int]
+    L.ray_tracing_gpu_overall.restype = ct.POINTER(ct.c_float)
+    L.ray_tracing_gpu_overall.argtypes = [ct.c_size_t, ct.c_size_t, np.ctypeslib.ndpointer(dtype=np.int32),
+                                          ct.c_size_t] + [np.ctypeslib.ndpointer(dtype=np.float32)] * 5 + [
+        ct.c_size_t, np.ctypeslib.ndpointer(dtype=np.float32), np.ctypeslib.ndpointer(dtype=np.float32), _i8ppp,
+        ct.POINTER(ct.c_int8), np.ctypeslib.ndpointer(dtype=np.int32), ct.c_int, ct.c_int, ct.c_int]
+    L.anacor_last_status.restype = ct.c_int
+    L.anacor_last_status.argtypes = []
+    L.anacor_last_error.restype = ct.c_char_p
+    L.anacor_last_error.argtypes = []
+    L.anacor_version.restype = ct.c_char_p
+    L.anacor_version.argtypes = []
+    L.anacor_absorption.restype = ct.c_int
+    L.anacor_absorption.argtypes = [_i8p, _i64p, _i64p, ct.c_int64, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p,
+                                    _f64p, _f64p, ct.c_int, ct.c_int, _f64p]
+    L.anacor_plan_create.restype = ct.c_void_p
+    L.anacor_plan_create.argtypes = [_i8p, _i64p, _i64p, ct.c_int64, _f64p, _f64p, ct.c_int, ct.c_int]
+    L.anacor_plan_set_reflections.restype = ct.c_int
+    L.anacor_plan_set_reflections.argtypes = [ct.c_void_p, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p]
+    L.anacor_plan_run.restype = ct.c_int
+    L.anacor_plan_run.argtypes = [ct.c_void_p, ct.c_void_p]
+    L.anacor_plan_result.restype = ct.c_int
+    L.anacor_plan_result.argtypes = [ct.c_void_p, _f64p, ct.c_void_p]
+    L.anacor_plan_device_result.restype = ct.c_void_p
+    L.anacor_plan_device_result.argtypes = [ct.c_void_p]
+    L.anacor_plan_n_refl.restype = ct.c_int64
+    L.anacor_plan_n_refl.argtypes = [ct.c_void_p]
+    L.anacor_plan_launch_info.restype = ct.c_int
+    L.anacor_plan_launch_info.argtypes = [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]
+    L.anacor_plan_count_steps.restype = ct.c_int
+    L.anacor_plan_count_steps.argtypes = [ct.c_void_p, ct.POINTER(ct.c_uint64)]
+    L.anacor_plan_destroy.restype = None
+    L.anacor_plan_destroy.argtypes = [ct.c_void_p]
+    L.anacor_batch_run.restype = ct.c_int
+    L.anacor_batch_run.argtypes = [ct.POINTER(ct.c_void_p), ct.c_int, ct.c_void_p]
+    L.anacor_rotated_vectors.restype = ct.c_int
+    L.anacor_rotated_vectors.argtypes = [_f64p, _f64p, _f64p, _f64p, _f64p, ct.c_int64, _f64p, _f64p]
+    L.anacor_leg_detail.restype = ct.c_int
+    L.anacor_leg_detail.argtypes = [_i8p, _i64p, _i64p, ct.c_int64, _f64p, _f64p, _f64p, ct.c_int,
+                                    _i32p, _i32p, _i32p, _i32p, _i32p, _f64p, _i32p]
+    L.free.restype = None
+    L.free.argtypes = [ct.c_void_p]
+    if path == _build.LIB:
+        _LIB = L
+    return L
+
+
+def last_error(L=None) -> tuple[int, str]:
+    L = L or load()
+    return int(L.anacor_last_status()), (L.anacor_last_error() or b"").decode()
+
+
+def check(status: int, L=None) -> None:
+    if status != 0:
+        st, msg = last_error(L)
+        raise AnacorError(status, msg)

@@ -1,0 +1,779 @@
+// C ABI of libanacor_gb300.so (declared in include/anacor_gb300.h).
+//
+// Host side of the path: argument checks, the FP64 per-reflection set-up
+// (reflection_setup.cpp), device buffers, launches and the reference's
+// ownership rules (malloc()ed result freed by the caller's free()).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "anacor_gb300.h"
+#include "anacor_internal.h"
+#include "trace_launch.h"
+
+using namespace anacor;
+
+namespace {
+
+thread_local int t_status = 0;
+thread_local std::string t_msg;
+
+int fail(int st, const std::string &msg)
+{
+    t_status = st;
+    t_msg = msg;
+    return st;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(kErrCuda, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int succeed()
+{
+    t_status = kOk;
+    t_msg.clear();
+    return kOk;
+}
+
+const char *status_text(int st)
+{
+    switch (st) {
+    case kErrNoFace: return "a ray found no exit plane";
+    case kErrAssert: return "exit face inconsistent with the ray angles (the reference asserts here)";
+    case kErrArgs: return "a coordinate lies outside the volume";
+    case kErrDirection: return "non-finite or zero direction vector";
+    default: return "error";
+    }
+}
+
+// ---------------------------------------------------------------- devices
+
+struct DeviceState {
+    bool ready = false;
+    int sms = 0;
+    int blocks_per_sm = 0;
+    cudaStream_t stream = nullptr;
+};
+
+std::mutex g_mu;
+DeviceState g_dev[64];
+
+int current_device(DeviceState **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "no usable CUDA device");
+    if (dev < 0 || dev >= 64)
+        return fail(kErrCuda, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    DeviceState &d = g_dev[dev];
+    if (!d.ready) {
+        cudaDeviceProp prop;
+        if ((e = cudaGetDeviceProperties(&prop, dev)) != cudaSuccess)
+            return cuda_fail(e, "cudaGetDeviceProperties");
+        if (prop.major < 10)
+            return fail(kErrCuda, "this library is built for sm_103a (Blackwell Ultra) only");
+        if (rcp_table_init() != kOk)
+            return fail(kErrCuda, "reciprocal table upload failed");
+        if (absorption_occupancy(&d.blocks_per_sm) != kOk || d.blocks_per_sm <= 0)
+            return fail(kErrCuda, "kernel not loadable on this device");
+        if ((e = cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_fail(e, "cudaStreamCreate");
+        d.sms = prop.multiProcessorCount;
+        d.ready = true;
+    }
+    *out = &d;
+    return kOk;
+}
+
+template <class T>
+cudaError_t dev_alloc(T **p, size_t count, cudaStream_t st)
+{
+    *p = nullptr;
+    if (count == 0)
+        return cudaSuccess;
+    return cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T), st);
+}
+
+template <class T>
+void dev_free(T *&p, cudaStream_t st)
+{
+    if (p)
+        cudaFreeAsync(p, st);
+    p = nullptr;
+}
+
+bool valid_shape(const int64_t *shape)
+{
+    for (int a = 0; a < 3; a++)
+        if (shape[a] <= 0 || shape[a] > kMaxDim)
+            return false;
+    return (uint64_t)shape[0] * shape[1] * shape[2] < (1ull << 31);
+}
+
+// Flat base of an int8*** row table built over a C-contiguous volume
+// (AnACor/utils/utils_os.py:45-68).  Returns nullptr if the rows are not one
+// uniformly strided block.
+const int8_t *flat_base(int8_t ***table, const int64_t *shape)
+{
+    if (!table || !table[0] || !table[0][0])
+        return nullptr;
+    const int8_t *base = table[0][0];
+    const int64_t Y = shape[1], X = shape[2];
+    for (int64_t z = 0; z < shape[0]; z++) {
+        if (!table[z])
+            return nullptr;
+        for (int64_t y = 0; y < Y; y++)
+            if (table[z][y] != base + (z * Y + y) * X)
+                return nullptr;
+    }
+    return base;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ plans
+
+struct anacor_plan {
+    int dims[3] = {0, 0, 0};
+    int n_vox = 0;
+    int full = 0, is_exp = 1;
+    double mu[4] = {0, 0, 0, 0};
+    double voxel[3] = {0, 0, 0};
+    cudaStream_t stream = nullptr;
+    DeviceState *dev = nullptr;
+    int8_t *d_vol = nullptr;
+    short4 *d_coords = nullptr;
+    ReflTable *d_refl = nullptr;
+    double *d_out = nullptr;
+    double *d_partial = nullptr;
+    unsigned *d_arrive = nullptr;
+    int *d_status = nullptr;
+    unsigned long long *d_counter = nullptr;
+    SampleDesc *d_desc = nullptr;
+    unsigned long long *d_steps = nullptr;
+    ReflTable *h_refl = nullptr;   // pinned staging
+    int64_t n_refl = 0, refl_cap = 0;
+    int tiles = 0;
+};
+
+namespace {
+
+void plan_release(anacor_plan *p)
+{
+    cudaStream_t st = p->stream;
+    dev_free(p->d_vol, st);
+    dev_free(p->d_coords, st);
+    dev_free(p->d_refl, st);
+    dev_free(p->d_out, st);
+    dev_free(p->d_partial, st);
+    dev_free(p->d_arrive, st);
+    dev_free(p->d_status, st);
+    dev_free(p->d_counter, st);
+    dev_free(p->d_desc, st);
+    dev_free(p->d_steps, st);
+    if (p->h_refl)
+        cudaFreeHost(p->h_refl);
+    p->h_refl = nullptr;
+    cudaStreamSynchronize(st);
+}
+
+int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
+              const double *voxel, const double *mu, int full, int is_exp)
+{
+    if (!label || !shape || !coords || !voxel || !mu)
+        return fail(kErrArgs, "null argument");
+    if (!valid_shape(shape))
+        return fail(kErrArgs, "volume axes must lie in [1, 8191] and the volume below 2^31 voxels");
+    if (n < 0 || n >= (1ll << 31))
+        return fail(kErrArgs, "coordinate count out of range");
+    DeviceState *dev = nullptr;
+    if (int st = current_device(&dev))
+        return st;
+    p->dev = dev;
+    p->stream = dev->stream;
+    for (int a = 0; a < 3; a++) {
+        p->dims[a] = (int)shape[a];
+        p->voxel[a] = voxel[a];
+    }
+    for (int a = 0; a < 4; a++)
+        p->mu[a] = mu[a];
+    p->n_vox = (int)n;
+    p->full = full;
+    p->is_exp = is_exp;
+    p->tiles = (int)((n + kTile - 1) / kTile);
+    cudaStream_t st = p->stream;
+    const size_t nvol = (size_t)shape[0] * shape[1] * shape[2];
+    cudaError_t e;
+    long long *d_c64 = nullptr;
+    if ((e = dev_alloc(&p->d_vol, nvol, st)) != cudaSuccess || (e = dev_alloc(&p->d_coords, (size_t)n, st)) ||
+        (e = dev_alloc(&p->d_status, 1, st)) || (e = dev_alloc(&p->d_counter, 1, st)) ||
+        (e = dev_alloc(&p->d_desc, 1, st)) || (e = dev_alloc(&d_c64, (size_t)n * 3, st)))
+        return cuda_fail(e, "device allocation");
+    if ((e = cudaMemcpyAsync(p->d_vol, label, nvol, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemsetAsync(p->d_status, 0, sizeof(int), st)))
+        return cuda_fail(e, "volume upload");
+    if (n > 0) {
+        if ((e = cudaMemcpyAsync(d_c64, coords, (size_t)n * 3 * sizeof(long long), cudaMemcpyHostToDevice, st)) ||
+            (e = launch_pack_coords(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)))
+            return cuda_fail(e, "coordinate upload");
+    }
+    dev_free(d_c64, st);
+    return kOk;
+}
+
+int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
+{
+    cudaStream_t st = p->stream;
+    cudaError_t e;
+    if (n_refl > p->refl_cap) {
+        dev_free(p->d_refl, st);
+        dev_free(p->d_out, st);
+        dev_free(p->d_partial, st);
+        dev_free(p->d_arrive, st);
+        if (p->h_refl) {
+            cudaStreamSynchronize(st);
+            cudaFreeHost(p->h_refl);
+            p->h_refl = nullptr;
+        }
+        if ((e = dev_alloc(&p->d_refl, (size_t)n_refl, st)) || (e = dev_alloc(&p->d_out, (size_t)n_refl, st)) ||
+            (e = dev_alloc(&p->d_partial, (size_t)n_refl * (size_t)std::max(p->tiles, 1), st)) ||
+            (e = dev_alloc(&p->d_arrive, (size_t)n_refl, st)))
+            return cuda_fail(e, "device allocation");
+        if ((e = cudaMemsetAsync(p->d_arrive, 0, (size_t)n_refl * sizeof(unsigned), st)))
+            return cuda_fail(e, "cudaMemset");
+        if ((e = cudaMallocHost(reinterpret_cast<void **>(&p->h_refl), (size_t)n_refl * sizeof(ReflTable))))
+            return cuda_fail(e, "pinned allocation");
+        p->refl_cap = n_refl;
+    }
+    p->n_refl = n_refl;
+    return kOk;
+}
+
+SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
+{
+    SampleDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.vol = p->d_vol;
+    for (int a = 0; a < 3; a++) {
+        d.dim[a] = p->dims[a];
+        d.voxel[a] = p->voxel[a];
+    }
+    for (int a = 0; a < 4; a++)
+        d.mu[a] = p->mu[a];
+    d.n_vox = p->n_vox;
+    d.coords = p->d_coords;
+    d.refl = p->d_refl;
+    d.n_refl = p->n_refl;
+    d.tiles = p->tiles;
+    d.full_iteration = p->full;
+    d.is_exp = p->is_exp;
+    d.out = p->d_out;
+    d.partial = p->d_partial;
+    d.arrive = p->d_arrive;
+    d.status = p->d_status;
+    d.work_begin = work_begin;
+    return d;
+}
+
+int plan_upload_desc(anacor_plan *p, unsigned long long *steps)
+{
+    cudaError_t e;
+    SampleDesc d = plan_desc(p, 0);
+    d.steps = steps;
+    if ((e = cudaMemcpyAsync(p->d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, p->stream)))
+        return cuda_fail(e, "descriptor upload");
+    // the descriptor lives on the stack: make sure it has been read
+    if ((e = cudaStreamSynchronize(p->stream)))
+        return cuda_fail(e, "upload");
+    return kOk;
+}
+
+// upload the staged tables and the plan's own one-sample descriptor
+int plan_upload_tables(anacor_plan *p)
+{
+    cudaError_t e;
+    if (p->n_refl > 0 &&
+        (e = cudaMemcpyAsync(p->d_refl, p->h_refl, (size_t)p->n_refl * sizeof(ReflTable), cudaMemcpyHostToDevice,
+                             p->stream)))
+        return cuda_fail(e, "table upload");
+    return plan_upload_desc(p, nullptr);
+}
+
+int plan_grid(const anacor_plan *p, long long items)
+{
+    const long long cap = (long long)p->dev->sms * p->dev->blocks_per_sm;
+    return (int)std::max(1ll, std::min(items, cap));
+}
+
+int plan_launch(anacor_plan *p, cudaStream_t st)
+{
+    const long long items = (long long)p->n_refl * p->tiles;
+    if (items == 0)
+        return kOk;
+    cudaError_t e = launch_absorption(p->d_desc, 1, items, p->d_counter, plan_grid(p, items), st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "kernel launch");
+    return kOk;
+}
+
+int plan_fetch(anacor_plan *p, double *out, cudaStream_t st)
+{
+    int status = 0;
+    cudaError_t e;
+    if (p->n_refl > 0 && p->n_vox > 0 &&
+        (e = cudaMemcpyAsync(out, p->d_out, (size_t)p->n_refl * sizeof(double), cudaMemcpyDeviceToHost, st)))
+        return cuda_fail(e, "result download");
+    if ((e = cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st)))
+        return cuda_fail(e, "result download");
+    if (p->n_vox == 0)
+        for (int64_t i = 0; i < p->n_refl; i++)
+            out[i] = std::nan("");   // the reference's 0/0 mean
+    if (status) {
+        for (int b = 1; b < 16; b++)
+            if (status & (1 << b))
+                return fail(b, status_text(b));
+    }
+    return succeed();
+}
+
+// transient plan: upload, set up, run, fetch (the drop-in entry points)
+int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, int64_t n, const double *voxel,
+             const double *mu, int full, int is_exp, const double *s1, const double *omega, int64_t n_refl,
+             const double *xray, const double *axis, const double *F, const ReflTable *tables, int threads,
+             double *out)
+{
+    anacor_plan p;
+    int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
+    if (!st)
+        st = plan_reserve_refl(&p, n_refl);
+    if (!st) {
+        if (tables)
+            std::memcpy(p.h_refl, tables, (size_t)n_refl * sizeof(ReflTable));
+        else if (n_refl > 0 && (st = setup_reflections(axis, omega, F, xray, s1, n_refl, p.h_refl, threads)))
+            fail(st, status_text(st));
+    }
+    if (!st)
+        st = plan_upload_tables(&p);
+    if (!st)
+        st = plan_launch(&p, p.stream);
+    if (!st)
+        st = plan_fetch(&p, out, p.stream);
+    const int keep = t_status;
+    const std::string msg = t_msg;
+    plan_release(&p);
+    t_status = keep;
+    t_msg = msg;
+    return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int anacor_last_status(void) { return t_status; }
+const char *anacor_last_error(void) { return t_msg.c_str(); }
+const char *anacor_version(void) { return "anacor_gb300 1.0 (sm_103a)"; }
+
+anacor_plan *anacor_plan_create(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
+                                const double *voxel, const double *mu, int full_iteration, int is_exp)
+{
+    anacor_plan *p = new (std::nothrow) anacor_plan();
+    if (!p) {
+        fail(kErrNoMem, "out of host memory");
+        return nullptr;
+    }
+    if (plan_init(p, label, shape, coords, n, voxel, mu, full_iteration, is_exp)) {
+        const int keep = t_status;
+        const std::string msg = t_msg;
+        if (p->stream)
+            plan_release(p);
+        delete p;
+        t_status = keep;
+        t_msg = msg;
+        return nullptr;
+    }
+    cudaError_t e = cudaStreamSynchronize(p->stream);
+    if (e != cudaSuccess) {
+        cuda_fail(e, "plan upload");
+        plan_release(p);
+        delete p;
+        return nullptr;
+    }
+    succeed();
+    return p;
+}
+
+int anacor_plan_set_reflections(anacor_plan *p, const double *s1, const double *omega, int64_t n_refl,
+                                const double *xray, const double *omega_axis, const double *F)
+{
+    if (!p || n_refl < 0 || (n_refl > 0 && (!s1 || !omega || !xray || !omega_axis || !F)))
+        return fail(kErrArgs, "bad arguments");
+    if (int st = plan_reserve_refl(p, n_refl))
+        return st;
+    if (n_refl > 0) {
+        if (int st = setup_reflections(omega_axis, omega, F, xray, s1, n_refl, p->h_refl, 0))
+            return fail(st, status_text(st));
+    }
+    if (int st = plan_upload_tables(p))
+        return st;
+    return succeed();
+}
+
+int anacor_plan_run(anacor_plan *p, void *stream)
+{
+    if (!p)
+        return fail(kErrArgs, "null plan");
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    if (int s = plan_launch(p, st))
+        return s;
+    return succeed();
+}
+
+int anacor_plan_result(anacor_plan *p, double *out, void *stream)
+{
+    if (!p || (!out && p->n_refl > 0))
+        return fail(kErrArgs, "bad arguments");
+    return plan_fetch(p, out, stream ? (cudaStream_t)stream : p->stream);
+}
+
+int anacor_plan_count_steps(anacor_plan *p, uint64_t *total)
+{
+    if (!p || !total)
+        return fail(kErrArgs, "bad arguments");
+    cudaError_t e;
+    if (!p->d_steps && (e = dev_alloc(&p->d_steps, 1, p->stream)))
+        return cuda_fail(e, "device allocation");
+    if ((e = cudaMemsetAsync(p->d_steps, 0, sizeof(unsigned long long), p->stream)))
+        return cuda_fail(e, "cudaMemset");
+    if (int st = plan_upload_desc(p, p->d_steps))
+        return st;
+    int st = plan_launch(p, p->stream);
+    unsigned long long h = 0;
+    if (!st && (e = cudaMemcpyAsync(&h, p->d_steps, sizeof(h), cudaMemcpyDeviceToHost, p->stream)))
+        st = cuda_fail(e, "download");
+    if (!st && (e = cudaStreamSynchronize(p->stream)))
+        st = cuda_fail(e, "count");
+    if (int s2 = plan_upload_desc(p, nullptr))
+        return s2;
+    if (st)
+        return st;
+    *total = h;
+    return succeed();
+}
+
+const double *anacor_plan_device_result(anacor_plan *p) { return p ? p->d_out : nullptr; }
+int64_t anacor_plan_n_refl(const anacor_plan *p) { return p ? p->n_refl : 0; }
+
+int anacor_plan_launch_info(const anacor_plan *p, int *grid, int *kernels)
+{
+    if (!p)
+        return fail(kErrArgs, "null plan");
+    const long long items = (long long)p->n_refl * p->tiles;
+    if (grid)
+        *grid = items ? plan_grid(p, items) : 0;
+    if (kernels)
+        *kernels = items ? 1 : 0;
+    return succeed();
+}
+
+void anacor_plan_destroy(anacor_plan *p)
+{
+    if (!p)
+        return;
+    plan_release(p);
+    delete p;
+}
+
+int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream)
+{
+    if (!plans || n_plans <= 0)
+        return fail(kErrArgs, "empty batch");
+    anacor_plan *p0 = plans[0];
+    cudaStream_t st = stream ? (cudaStream_t)stream : p0->stream;
+    std::vector<SampleDesc> descs;
+    long long total = 0;
+    for (int i = 0; i < n_plans; i++) {
+        if (!plans[i])
+            return fail(kErrArgs, "null plan in batch");
+        descs.push_back(plan_desc(plans[i], total));
+        total += (long long)plans[i]->n_refl * plans[i]->tiles;
+    }
+    // batch descriptors live in a device buffer owned by the first plan's device state
+    static thread_local SampleDesc *d_descs = nullptr;
+    static thread_local int d_cap = 0;
+    cudaError_t e;
+    if (n_plans > d_cap) {
+        if (d_descs)
+            cudaFree(d_descs);
+        if ((e = cudaMalloc(&d_descs, sizeof(SampleDesc) * (size_t)n_plans)))
+            return cuda_fail(e, "device allocation");
+        d_cap = n_plans;
+    }
+    if ((e = cudaMemcpyAsync(d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice, st)))
+        return cuda_fail(e, "descriptor upload");
+    if (total > 0) {
+        const int grid = plan_grid(p0, total);
+        if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st)))
+            return cuda_fail(e, "kernel launch");
+    }
+    if ((e = cudaStreamSynchronize(st)))
+        return cuda_fail(e, "batch");
+    return succeed();
+}
+
+int anacor_absorption(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n_coords,
+                      const double *s1, const double *omega, int64_t n_refl, const double *xray,
+                      const double *omega_axis, const double *F, const double *voxel, const double *mu,
+                      int full_iteration, int is_exp, double *out)
+{
+    if (n_refl < 0 || (n_refl > 0 && (!s1 || !omega || !xray || !omega_axis || !F || !out)))
+        return fail(kErrArgs, "bad arguments");
+    return run_once(label, shape, coords, n_coords, voxel, mu, full_iteration, is_exp, s1, omega, n_refl, xray,
+                    omega_axis, F, nullptr, 0, out);
+}
+
+double *ray_tracing_overall(int64_t low, int64_t up, int64_t *coord_list, int64_t len_coord_list,
+                            const double *scattering_vector_list, const double *omega_list,
+                            const double *raw_xray, const double *omega_axis, const double *kp_rotation_matrix,
+                            int64_t len_result, double *voxel_size, double *coefficients, int8_t ***label_list,
+                            int64_t *shape, int full_iteration, int store_paths, int num_workers, int IsExp)
+{
+    (void)low; (void)up; (void)store_paths;
+    if (!shape || !valid_shape(shape)) {
+        fail(kErrArgs, "volume axes must lie in [1, 8191] and the volume below 2^31 voxels");
+        return nullptr;
+    }
+    if (len_result < 0 || !scattering_vector_list || !omega_list || !raw_xray || !omega_axis ||
+        !kp_rotation_matrix || !voxel_size || !coefficients || !coord_list) {
+        fail(kErrArgs, "bad arguments");
+        return nullptr;
+    }
+    std::vector<int8_t> gathered;
+    const int8_t *flat = flat_base(label_list, shape);
+    if (!flat) {
+        if (!label_list) {
+            fail(kErrArgs, "null label table");
+            return nullptr;
+        }
+        // rows are not one strided block: gather them
+        gathered.resize((size_t)shape[0] * shape[1] * shape[2]);
+        for (int64_t z = 0; z < shape[0]; z++)
+            for (int64_t y = 0; y < shape[1]; y++)
+                std::memcpy(&gathered[(z * shape[1] + y) * shape[2]], label_list[z][y], (size_t)shape[2]);
+        flat = gathered.data();
+    }
+    double *result = static_cast<double *>(std::malloc((size_t)std::max<int64_t>(len_result, 1) * sizeof(double)));
+    if (!result) {
+        fail(kErrNoMem, "out of host memory");
+        return nullptr;
+    }
+    const int is_exp = (signed char)IsExp == 1;   // the reference passes it on as char
+    if (run_once(flat, shape, coord_list, len_coord_list, voxel_size, coefficients, full_iteration, is_exp,
+                 scattering_vector_list, omega_list, len_result, raw_xray, omega_axis, kp_rotation_matrix, nullptr,
+                 num_workers, result)) {
+        std::free(result);
+        return nullptr;
+    }
+    return result;
+}
+
+double ray_tracing_single(int64_t *coord_list, int64_t len_coord_list, const double *rotated_s1,
+                          const double *xray, double *voxel_size, double *coefficients, int8_t ***label_list,
+                          int64_t *shape, int full_iteration, int64_t store_paths, int IsExp)
+{
+    (void)store_paths;
+    const double nan = std::nan("");
+    if (!shape || !valid_shape(shape) || !rotated_s1 || !xray || !voxel_size || !coefficients || !coord_list) {
+        fail(kErrArgs, "bad arguments");
+        return nan;
+    }
+    std::vector<int8_t> gathered;
+    const int8_t *flat = flat_base(label_list, shape);
+    if (!flat) {
+        if (!label_list) {
+            fail(kErrArgs, "null label table");
+            return nan;
+        }
+        gathered.resize((size_t)shape[0] * shape[1] * shape[2]);
+        for (int64_t z = 0; z < shape[0]; z++)
+            for (int64_t y = 0; y < shape[1]; y++)
+                std::memcpy(&gathered[(z * shape[1] + y) * shape[2]], label_list[z][y], (size_t)shape[2]);
+        flat = gathered.data();
+    }
+    ReflTable tab;
+    if (int st = setup_rotated(xray, rotated_s1, &tab)) {
+        fail(st, status_text(st));
+        return nan;
+    }
+    double out = nan;
+    const int is_exp = (signed char)IsExp == 1;
+    if (run_once(flat, shape, coord_list, len_coord_list, voxel_size, coefficients, full_iteration, is_exp, nullptr,
+                 nullptr, 1, nullptr, nullptr, nullptr, &tab, 0, &out))
+        return nan;
+    return out;
+}
+
+double ib_test(int64_t *coord_list, int64_t len_coord_list, double *rotated_s1, double *xray, double *voxel_size,
+               double *coefficients, int8_t ***label_list, int64_t *shape, int full_iteration, int64_t store_paths,
+               int num_cls)
+{
+    (void)coord_list; (void)len_coord_list; (void)rotated_s1; (void)xray; (void)voxel_size;
+    (void)coefficients; (void)label_list; (void)shape; (void)full_iteration; (void)store_paths; (void)num_cls;
+    fail(kErrUnsupported, "ib_test: the iterative-bisection method is not provided by this library");
+    return std::nan("");
+}
+
+float *ray_tracing_gpu_overall(size_t low, size_t up, int *coord_list, size_t len_coord_list,
+                               const float *scattering_vector_list, const float *omega_list, const float *raw_xray,
+                               const float *omega_axis, const float *kp_rotation_matrix, size_t len_result,
+                               float *voxel_size, float *coefficients, int8_t ***label_list, int8_t *label_list_1d,
+                               int *shape, int full_iteration, int store_paths, int gpumethod)
+{
+    (void)gpumethod;
+    if (!shape || !coord_list || !scattering_vector_list || !omega_list || !raw_xray || !omega_axis ||
+        !kp_rotation_matrix || !voxel_size || !coefficients) {
+        fail(kErrArgs, "bad arguments");
+        return nullptr;
+    }
+    int64_t shp[3] = {shape[0], shape[1], shape[2]};
+    if (!valid_shape(shp)) {
+        fail(kErrArgs, "volume axes must lie in [1, 8191] and the volume below 2^31 voxels");
+        return nullptr;
+    }
+    std::vector<int64_t> c((size_t)len_coord_list * 3);
+    for (size_t i = 0; i < c.size(); i++)
+        c[i] = coord_list[i];
+    std::vector<double> s1(len_result * 3), om(len_result);
+    for (size_t i = 0; i < len_result * 3; i++)
+        s1[i] = scattering_vector_list[i];
+    for (size_t i = 0; i < len_result; i++)
+        om[i] = omega_list[i];
+    double xr[3], ax[3], F[9], vox[3], mu[4];
+    for (int a = 0; a < 3; a++) {
+        xr[a] = raw_xray[a];
+        ax[a] = omega_axis[a];
+        vox[a] = voxel_size[a];
+    }
+    for (int a = 0; a < 9; a++)
+        F[a] = kp_rotation_matrix[a];
+    for (int a = 0; a < 4; a++)
+        mu[a] = coefficients[a];
+    std::vector<int8_t> gathered;
+    const int8_t *flat = label_list_1d ? label_list_1d : flat_base(label_list, shp);
+    if (!flat) {
+        if (!label_list) {
+            fail(kErrArgs, "null label table");
+            return nullptr;
+        }
+        gathered.resize((size_t)shp[0] * shp[1] * shp[2]);
+        for (int64_t z = 0; z < shp[0]; z++)
+            for (int64_t y = 0; y < shp[1]; y++)
+                std::memcpy(&gathered[(z * shp[1] + y) * shp[2]], label_list[z][y], (size_t)shp[2]);
+        flat = gathered.data();
+    }
+    std::vector<double> res(std::max<size_t>(len_result, 1));
+    (void)low; (void)up; (void)store_paths;
+    if (run_once(flat, shp, c.data(), (int64_t)len_coord_list, vox, mu, full_iteration, 1, s1.data(), om.data(),
+                 (int64_t)len_result, xr, ax, F, nullptr, 0, res.data()))
+        return nullptr;
+    float *out = static_cast<float *>(std::malloc(std::max<size_t>(len_result, 1) * sizeof(float)));
+    if (!out) {
+        fail(kErrNoMem, "out of host memory");
+        return nullptr;
+    }
+    for (size_t i = 0; i < len_result; i++)
+        out[i] = (float)res[i];
+    return out;
+}
+
+int anacor_rotated_vectors(const double *omega_axis, const double *omega, const double *F, const double *xray,
+                           const double *s1, int64_t n, double *rx, double *rs)
+{
+    if (!omega_axis || !omega || !F || !xray || !s1 || !rx || !rs || n < 0)
+        return fail(kErrArgs, "bad arguments");
+    ReflTable tab;
+    for (int64_t i = 0; i < n; i++)
+        setup_reflection(omega_axis, omega[i], F, xray, s1 + 3 * i, &tab, rx + 3 * i, rs + 3 * i);
+    return succeed();
+}
+
+int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
+                      const double *rotated_s1, const double *rotated_xray, const double *voxel,
+                      int full_iteration, int32_t *face, int32_t *len, int32_t *nseg, int32_t *first,
+                      int32_t *last, double *L, int32_t *status)
+{
+    if (!face || !len || !nseg || !first || !last || !L || !status || !rotated_s1 || !rotated_xray)
+        return fail(kErrArgs, "bad arguments");
+    ReflTable tab;
+    if (int st = setup_rotated(rotated_xray, rotated_s1, &tab))
+        return fail(st, status_text(st));
+    static const double mu0[4] = {0, 0, 0, 0};
+    anacor_plan p;
+    int st = plan_init(&p, label, shape, coords, n, voxel, mu0, full_iteration, 1);
+    ReflTable *d_tab = nullptr;
+    double *d_vox = nullptr;
+    int *d_i = nullptr;
+    double *d_L = nullptr;
+    cudaError_t e = cudaSuccess;
+    const size_t m = (size_t)std::max<int64_t>(n, 1) * 2;
+    if (!st) {
+        if ((e = dev_alloc(&d_tab, 1, p.stream)) || (e = dev_alloc(&d_vox, 3, p.stream)) ||
+            (e = dev_alloc(&d_i, m * 10, p.stream)) || (e = dev_alloc(&d_L, m * 4, p.stream)) ||
+            (e = cudaMemcpyAsync(d_tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, p.stream)) ||
+            (e = cudaMemcpyAsync(d_vox, voxel, 3 * sizeof(double), cudaMemcpyHostToDevice, p.stream)) ||
+            (e = launch_leg_detail(d_tab, p.d_vol, p.dims, p.d_coords, (int)n, d_vox, full_iteration, d_i,
+                                   d_i + m, d_i + 2 * m, d_i + 3 * m, d_i + 6 * m, d_L, d_i + 9 * m, p.stream)))
+            st = cuda_fail(e, "leg detail");
+    }
+    if (!st && n > 0) {
+        std::vector<int32_t> h(m * 10);
+        if ((e = cudaMemcpyAsync(h.data(), d_i, m * 10 * sizeof(int), cudaMemcpyDeviceToHost, p.stream)) ||
+            (e = cudaMemcpyAsync(L, d_L, (size_t)n * 2 * 4 * sizeof(double), cudaMemcpyDeviceToHost, p.stream)) ||
+            (e = cudaStreamSynchronize(p.stream)))
+            st = cuda_fail(e, "leg detail download");
+        else {
+            const size_t k = (size_t)n * 2;
+            std::memcpy(face, h.data(), k * sizeof(int32_t));
+            std::memcpy(len, h.data() + m, k * sizeof(int32_t));
+            std::memcpy(nseg, h.data() + 2 * m, k * sizeof(int32_t));
+            std::memcpy(first, h.data() + 3 * m, 3 * k * sizeof(int32_t));
+            std::memcpy(last, h.data() + 6 * m, 3 * k * sizeof(int32_t));
+            std::memcpy(status, h.data() + 9 * m, k * sizeof(int32_t));
+        }
+    }
+    if (!st) {
+        int dst = 0;
+        if ((e = cudaMemcpy(&dst, p.d_status, sizeof(int), cudaMemcpyDeviceToHost)))
+            st = cuda_fail(e, "status");
+        else if (dst & (1 << kErrArgs))
+            st = fail(kErrArgs, status_text(kErrArgs));
+    }
+    const int keep = t_status;
+    const std::string msg = t_msg;
+    if (p.stream) {
+        dev_free(d_tab, p.stream);
+        dev_free(d_vox, p.stream);
+        dev_free(d_i, p.stream);
+        dev_free(d_L, p.stream);
+        plan_release(&p);
+    }
+    if (st) {
+        t_status = keep;
+        t_msg = msg;
+        return st;
+    }
+    return succeed();
+}
+
+}  // extern "C"

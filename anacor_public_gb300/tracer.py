@@ -1,0 +1,143 @@
+"""Python front end of the GPU absorption path (numpy in, numpy out).
+
+``absorption(...)``   one-shot A_h for a sample (uploads, runs, downloads);
+``Plan``              device-resident sample for repeated or timed runs;
+``batch_run(plans)``  one persistent launch over several samples;
+``leg_detail(...)``   per-voxel march detail of one reflection (parity checks);
+``rotated_vectors``   the host set-up's rotated incident / diffracted vectors.
+
+All compute happens in libanacor_gb300.so on the current CUDA device.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import _lib
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def absorption(label, coords, s1, omega, xray, omega_axis, F, voxel, mu, full_iteration=0, is_exp=1):
+    L = _lib.load()
+    label = _c(label, np.int8)
+    s1 = _c(s1, np.float64).reshape(-1, 3)
+    n = s1.shape[0]
+    out = np.zeros(max(n, 1), dtype=np.float64)
+    st = L.anacor_absorption(label, np.array(label.shape, dtype=np.int64), _c(coords, np.int64).reshape(-1, 3),
+                             len(coords), s1, _c(omega, np.float64), n, _c(xray, np.float64),
+                             _c(omega_axis, np.float64), _c(F, np.float64).reshape(-1), _c(voxel, np.float64),
+                             _c(mu, np.float64), int(full_iteration), int(is_exp), out)
+    _lib.check(st, L)
+    return out[:n]
+
+
+def sample_absorption(s, **kw):
+    return absorption(s.label, s.coords, s.s1, s.omega, s.xray, s.omega_axis, s.F, s.voxel, s.mu, **kw)
+
+
+class Plan:
+    """A sample resident in device memory: volume, voxel list, reflection tables."""
+
+    def __init__(self, label, coords, voxel, mu, full_iteration=0, is_exp=1):
+        self._L = _lib.load()
+        label = _c(label, np.int8)
+        self.shape = label.shape
+        self.n_vox = len(coords)
+        h = self._L.anacor_plan_create(label, np.array(label.shape, dtype=np.int64),
+                                       _c(coords, np.int64).reshape(-1, 3), len(coords), _c(voxel, np.float64),
+                                       _c(mu, np.float64), int(full_iteration), int(is_exp))
+        if not h:
+            st, msg = _lib.last_error(self._L)
+            raise _lib.AnacorError(st, msg)
+        self._h = ct.c_void_p(h)
+        self.n_refl = 0
+
+    @classmethod
+    def from_sample(cls, s, **kw):
+        p = cls(s.label, s.coords, s.voxel, s.mu, **kw)
+        p.set_reflections(s.s1, s.omega, s.xray, s.omega_axis, s.F)
+        return p
+
+    def set_reflections(self, s1, omega, xray, omega_axis, F):
+        s1 = _c(s1, np.float64).reshape(-1, 3)
+        st = self._L.anacor_plan_set_reflections(self._h, s1, _c(omega, np.float64), s1.shape[0],
+                                                 _c(xray, np.float64), _c(omega_axis, np.float64),
+                                                 _c(F, np.float64).reshape(-1))
+        _lib.check(st, self._L)
+        self.n_refl = s1.shape[0]
+
+    def run(self, stream: int | None = None):
+        """Enqueue the march on `stream` (a raw cudaStream_t handle) or the plan's own stream."""
+        _lib.check(self._L.anacor_plan_run(self._h, ct.c_void_p(stream or 0)), self._L)
+
+    def result(self, stream: int | None = None) -> np.ndarray:
+        out = np.zeros(max(self.n_refl, 1), dtype=np.float64)
+        _lib.check(self._L.anacor_plan_result(self._h, out, ct.c_void_p(stream or 0)), self._L)
+        return out[:self.n_refl]
+
+    def device_result_ptr(self) -> int:
+        return int(self._L.anacor_plan_device_result(self._h) or 0)
+
+    def count_steps(self) -> int:
+        """Sum of len_path_2 over every ray (one extra run with counting on)."""
+        n = ct.c_uint64()
+        _lib.check(self._L.anacor_plan_count_steps(self._h, ct.byref(n)), self._L)
+        return int(n.value)
+
+    def launch_info(self):
+        g, k = ct.c_int(), ct.c_int()
+        _lib.check(self._L.anacor_plan_launch_info(self._h, ct.byref(g), ct.byref(k)), self._L)
+        return g.value, k.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.anacor_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_run(plans, stream: int | None = None):
+    L = _lib.load()
+    arr = (ct.c_void_p * len(plans))(*[p._h.value for p in plans])
+    _lib.check(L.anacor_batch_run(arr, len(plans), ct.c_void_p(stream or 0)), L)
+
+
+def rotated_vectors(omega_axis, omega, F, xray, s1):
+    L = _lib.load()
+    s1 = _c(s1, np.float64).reshape(-1, 3)
+    n = s1.shape[0]
+    rx = np.zeros((max(n, 1), 3))
+    rs = np.zeros((max(n, 1), 3))
+    _lib.check(L.anacor_rotated_vectors(_c(omega_axis, np.float64), _c(omega, np.float64),
+                                        _c(F, np.float64).reshape(-1), _c(xray, np.float64), s1, n, rx, rs), L)
+    return rx[:n], rs[:n]
+
+
+def leg_detail(label, coords, s1_rot, xray_rot, voxel, full_iteration=0) -> dict:
+    L = _lib.load()
+    label = _c(label, np.int8)
+    coords = _c(coords, np.int64).reshape(-1, 3)
+    n = len(coords)
+    m = max(n, 1)
+    face = np.zeros((m, 2), np.int32)
+    ln = np.zeros((m, 2), np.int32)
+    nseg = np.zeros((m, 2), np.int32)
+    first = np.zeros((m, 2, 3), np.int32)
+    last = np.zeros((m, 2, 3), np.int32)
+    Ls = np.zeros((m, 2, 4), np.float64)
+    status = np.zeros((m, 2), np.int32)
+    st = L.anacor_leg_detail(label, np.array(label.shape, dtype=np.int64), coords, n, _c(s1_rot, np.float64),
+                             _c(xray_rot, np.float64), _c(voxel, np.float64), int(full_iteration), face, ln, nseg,
+                             first, last, Ls, status)
+    _lib.check(st, L)
+    return dict(face=face[:n], len=ln[:n], nseg=nseg[:n], first=first[:n], last=last[:n], L=Ls[:n],
+                status=status[:n])

@@ -1,0 +1,156 @@
+/*
+ * anacor_gb300.h -- C ABI of libanacor_gb300.so, the GB300 (sm_103a)
+ * implementation of AnACor's analytical absorption-correction path.
+ *
+ * The first four entry points have exactly the signatures of the reference
+ * library that AnACor's worker loads with ctypes (AnACor/utils/utils_mp.py:51-148),
+ * so the library is a drop-in for AnACor/src/ray_tracing_cpu.so on that path.
+ * Everything runs on the current CUDA device; there is no CPU fallback: when
+ * no usable GPU is present every entry point fails with a status and a
+ * message (anacor_last_error) instead of computing on the host.
+ *
+ * Conventions (same as the reference): coordinates are int64 (z, y, x) rows,
+ * C-contiguous; shape is (z, y, x); voxel_size is (z, y, x); coefficients are
+ * [liquor, loop, crystal, bubble]; label codes 0 vacuum, 1 liquor, 2 loop,
+ * 3 crystal, 4 bubble; vectors are in the DIALS laboratory frame.
+ */
+#ifndef ANACOR_GB300_H
+#define ANACOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ drop-ins -- */
+
+/* Replaces AnACor/src/ray_tracing.c:365-374 (ray_tracing_overall).
+ * Absorption factor A_h of reflections [0, len_result) (low/up are labels
+ * only, as in the reference).  For reflection i the incident and diffracted
+ * vectors are rotated by (R(omega_axis, omega_list[i]) * kp_rotation_matrix)^T
+ * and A_i is the mean over the len_coord_list voxels of exp(-sum mu_m L_m).
+ * label_list is the int8*** row table of a C-contiguous volume
+ * (AnACor/utils/utils_os.py:45-68).  num_workers and store_paths are
+ * accepted and ignored.  IsExp == 1 gives exp(-mu L), otherwise mu L.
+ * Returns a malloc()ed double[len_result] that the caller releases with the C
+ * library's free(), or NULL on error (see anacor_last_error). */
+double *ray_tracing_overall(int64_t low, int64_t up, int64_t *coord_list, int64_t len_coord_list,
+                            const double *scattering_vector_list, const double *omega_list,
+                            const double *raw_xray, const double *omega_axis, const double *kp_rotation_matrix,
+                            int64_t len_result, double *voxel_size, double *coefficients,
+                            int8_t ***label_list, int64_t *shape, int full_iteration, int store_paths,
+                            int num_workers, int IsExp);
+
+/* Replaces AnACor/src/ray_tracing.c:166-171 (ray_tracing_single): A_h of one
+ * reflection from already rotated vectors.  Returns NaN on error. */
+double ray_tracing_single(int64_t *coord_list, int64_t len_coord_list, const double *rotated_s1,
+                          const double *xray, double *voxel_size, double *coefficients, int8_t ***label_list,
+                          int64_t *shape, int full_iteration, int64_t store_paths, int IsExp);
+
+/* Symbol of AnACor/src/ray_tracing.c:25-31 (ib_test, the iterative-bisection
+ * variant).  AnACor's worker binds it at load time (utils_mp.py:95-109), so
+ * it is exported; the bisection method is not part of this library and the
+ * call returns NaN with status ANACOR_ERR_UNSUPPORTED. */
+double ib_test(int64_t *coord_list, int64_t len_coord_list, double *rotated_s1, double *xray,
+               double *voxel_size, double *coefficients, int8_t ***label_list, int64_t *shape,
+               int full_iteration, int64_t store_paths, int num_cls);
+
+/* Replaces AnACor/src/ray_tracing_gpu.c:33-42 (ray_tracing_gpu_overall, the
+ * FP32 ABI of the reference's CUDA library).  Inputs are widened to double
+ * and the same path runs; label_list_1d (the flat volume) is used when
+ * non-NULL, else label_list.  gpumethod is ignored.  Returns a malloc()ed
+ * float[len_result], or NULL on error. */
+float *ray_tracing_gpu_overall(size_t low, size_t up, int *coord_list, size_t len_coord_list,
+                               const float *scattering_vector_list, const float *omega_list,
+                               const float *raw_xray, const float *omega_axis, const float *kp_rotation_matrix,
+                               size_t len_result, float *voxel_size, float *coefficients, int8_t ***label_list,
+                               int8_t *label_list_1d, int *shape, int full_iteration, int store_paths,
+                               int gpumethod);
+
+/* --------------------------------------------------------------- status -- */
+
+enum {
+    ANACOR_OK = 0,
+    ANACOR_ERR_NO_FACE = 1,     /* a ray found no exit plane (reference: exit()) */
+    ANACOR_ERR_ASSERT = 2,      /* face/angle combination the reference asserts on */
+    ANACOR_ERR_ARGS = 3,
+    ANACOR_ERR_CUDA = 4,
+    ANACOR_ERR_NOMEM = 5,
+    ANACOR_ERR_UNSUPPORTED = 6,
+    ANACOR_ERR_DIRECTION = 7    /* non-finite or zero direction */
+};
+
+/* Status and message of the calling thread's last call (no counterpart in
+ * the reference, which aborts the process instead). */
+int anacor_last_status(void);
+const char *anacor_last_error(void);
+const char *anacor_version(void);
+
+/* ------------------------------------------------------ flat-buffer API -- */
+
+/* ray_tracing_overall over flat buffers: label is the C-contiguous int8
+ * volume itself instead of a row table.  Writes A_h to out[n_refl].
+ * Returns a status.  (No reference counterpart: the reference only takes the
+ * int8*** table.) */
+int anacor_absorption(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n_coords,
+                      const double *s1, const double *omega, int64_t n_refl, const double *xray,
+                      const double *omega_axis, const double *F, const double *voxel, const double *mu,
+                      int full_iteration, int is_exp, double *out);
+
+/* ------------------------------------------------------- resident plans -- */
+
+/* A plan keeps one sample's volume, voxel list and reflection tables in
+ * device memory so that the march can be re-run without host traffic.
+ * (No reference counterpart.) */
+typedef struct anacor_plan anacor_plan;
+
+anacor_plan *anacor_plan_create(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n_coords,
+                                const double *voxel, const double *mu, int full_iteration, int is_exp);
+/* Host FP64 set-up of n_refl reflections and upload of their tables. */
+int anacor_plan_set_reflections(anacor_plan *p, const double *s1, const double *omega, int64_t n_refl,
+                                const double *xray, const double *omega_axis, const double *F);
+/* Enqueue the march on `stream` (a cudaStream_t, NULL for the plan's own
+ * stream).  Results stay on the device. */
+int anacor_plan_run(anacor_plan *p, void *stream);
+/* Copy the last results to out[n_refl], synchronise and check the device
+ * status word. */
+int anacor_plan_result(anacor_plan *p, double *out, void *stream);
+/* Device pointer of the result array (valid until the plan is destroyed or
+ * its reflections change). */
+const double *anacor_plan_device_result(anacor_plan *p);
+int64_t anacor_plan_n_refl(const anacor_plan *p);
+/* Run once with step counting: *total = sum of len_path_2 over every ray of
+ * every reflection (the label bytes the reference's march reads). */
+int anacor_plan_count_steps(anacor_plan *p, uint64_t *total);
+/* Number of CTAs one run launches and the number of kernels it enqueues. */
+int anacor_plan_launch_info(const anacor_plan *p, int *grid, int *kernels);
+void anacor_plan_destroy(anacor_plan *p);
+
+/* One persistent launch over several plans (independent samples with their
+ * own volumes, voxel lists and reflections).  Results land in each plan. */
+int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream);
+
+/* ---------------------------------------------------------- diagnostics -- */
+
+/* Rotated incident and diffracted vectors of n reflections, computed by the
+ * host set-up code (AnACor/src/ray_tracing.c:397-407). */
+int anacor_rotated_vectors(const double *omega_axis, const double *omega, const double *F, const double *xray,
+                           const double *s1, int64_t n, double *rotated_xray, double *rotated_s1);
+
+/* Per-voxel, per-leg march detail of one reflection (rotated vectors as for
+ * ray_tracing_single), computed on the GPU: exit face, path length in steps
+ * (len_path_2), number of class segments, first and last path point and the
+ * four material lengths.  Arrays are [n][2] (leg 0 incident, leg 1
+ * diffracted), points [n][2][3], lengths [n][2][4]. */
+int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
+                      const double *rotated_s1, const double *rotated_xray, const double *voxel,
+                      int full_iteration, int32_t *face, int32_t *len, int32_t *nseg, int32_t *first,
+                      int32_t *last, double *L, int32_t *status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ANACOR_GB300_H */

@@ -1,0 +1,130 @@
+"""Generate the golden fixtures in this directory from the reference library.
+
+Run in a container that holds the reference sources (they are compiled by
+``make -C oracle ref`` into ``oracle/_ref/ray_tracing_cpu.so``):
+
+    python tests/golden/make_golden.py
+
+Fixtures (all small):
+  small_ah.npz      A_h of every reflection of the 96^3 sample (seed 0, 300
+                    reflections, all crystal voxels) from the reference's
+                    ray_tracing_overall, plus checksums of the generated inputs.
+  small_legs.npz    per-voxel, per-leg detail (exit face, len_path_2, number of
+                    class segments, last path point, four lengths) from the
+                    reference's cube_face / cal_coord / cal_path2_plus for a
+                    voxel subset of 8 reflections.
+  beamline_ah.npz   A_h of 12 reflections of the 512x512x400 stride-4 sample.
+  sphere_kat.npz    A_h of a voxelised sphere at mu*r = 0.1, 0.5, 1 and
+                    2theta = linspace(0, 180, 10), from the reference's
+                    ray_tracing_single, beside the analytic transmission values
+                    that AnACor/verification/sphere_verification_new.py:31-36
+                    checks against.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from anacor_public_gb300 import synth  # noqa: E402
+from oracle import oracle as orc  # noqa: E402
+
+# analytic sphere transmission factors at 2theta = linspace(0, 180, 10)
+# (AnACor/verification/sphere_verification_new.py:31-36)
+SPHERE_ANALYTIC = {
+    0.1: [0.86140064, 0.86140064, 0.8616233, 0.86206897, 0.86258949,
+          0.86311065, 0.86363244, 0.86415486, 0.86445367, 0.8645284],
+    0.5: [0.48181161, 0.4829518, 0.48626307, 0.49164208, 0.49860391,
+          0.50645733, 0.51427102, 0.52099614, 0.52565181, 0.52731491],
+    1.0: [0.24250067, 0.24500796, 0.25236593, 0.26373395, 0.27777006,
+          0.29295445, 0.30770178, 0.32034854, 0.32913142, 0.33233632],
+}
+SPHERE_RADIUS = 24          # voxels
+SPHERE_VOXEL = 0.5          # um
+
+
+def digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(str(a.dtype).encode())
+        h.update(str(a.shape).encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def sample_digest(s) -> str:
+    return digest(s.label, s.coords, s.s1, s.omega, s.xray, s.omega_axis, s.F, s.voxel, s.mu)
+
+
+def sphere_volume(radius: int):
+    n = 3 * radius
+    c = n / 2 - 1
+    g = np.arange(n, dtype=np.float64) - c
+    zz, yy, xx = np.meshgrid(g, g, g, indexing="ij", sparse=True)
+    vol = np.where(zz ** 2 + yy ** 2 + xx ** 2 < radius ** 2, 3, 0).astype(np.int8)
+    return np.ascontiguousarray(vol)
+
+
+def sphere_directions(two_theta_deg):
+    """Rotated incident / diffracted vectors at scattering angle 2theta, in a
+    generic orientation (no exactly-zero component)."""
+    rot = synth.euler_matrix(0.3, 1.1, 2.0)
+    b = np.array([-1.0, 0.0, 0.0])
+    out = []
+    for t in np.deg2rad(two_theta_deg):
+        s = np.array([-np.cos(t), np.sin(t) * 0.6, np.sin(t) * 0.8])
+        out.append((rot @ b, rot @ s))
+    return out
+
+
+def main():
+    orc.build_oracle(ref=True)
+    ref = orc.Reference()
+
+    s = synth.small_sample()
+    ah = ref.overall(s, num_workers=os.cpu_count() or 1)
+    np.savez_compressed(os.path.join(HERE, "small_ah.npz"), ah=ah, digest=sample_digest(s))
+
+    o = orc.Oracle()
+    legs = {k: [] for k in ("refl", "face", "len", "nseg", "last", "L")}
+    sel = np.ascontiguousarray(s.coords[::23])
+    for i in range(0, s.n_refl, 37):
+        xr, sr = o.rotate(s, i)
+        d = ref.leg_detail(sel, sr, xr, s.voxel, s.label)
+        legs["refl"].append(i)
+        for k in ("face", "len", "nseg", "last", "L"):
+            legs[k].append(d[k])
+    np.savez_compressed(os.path.join(HERE, "small_legs.npz"), coords=sel,
+                        **{k: np.array(v) for k, v in legs.items()})
+
+    b = synth.beamline_sample(n_refl=12)
+    ahb = ref.overall(b, num_workers=os.cpu_count() or 1)
+    np.savez_compressed(os.path.join(HERE, "beamline_ah.npz"), ah=ahb, digest=sample_digest(b))
+
+    vol = sphere_volume(SPHERE_RADIUS)
+    coords = np.ascontiguousarray(np.argwhere(vol == 3).astype(np.int64))[::7]
+    tth = np.linspace(0, 180, 10)
+    res = {}
+    voxel = np.array([SPHERE_VOXEL] * 3)
+    for mur in (0.1, 0.5, 1.0):
+        mu = np.array([0.0, 0.0, mur / (SPHERE_RADIUS * SPHERE_VOXEL), 0.0])
+        res[mur] = [ref.single(coords, sr, xr, voxel, mu, vol) for xr, sr in sphere_directions(tth)]
+    np.savez_compressed(os.path.join(HERE, "sphere_kat.npz"), coords=coords, two_theta=tth,
+                        mur=np.array([0.1, 0.5, 1.0]),
+                        reference=np.array([res[m] for m in (0.1, 0.5, 1.0)]),
+                        analytic=np.array([SPHERE_ANALYTIC[m] for m in (0.1, 0.5, 1.0)]))
+    print("small_ah", ah[:4], "beamline", ahb[:4])
+    for m in (0.1, 0.5, 1.0):
+        err = np.abs(np.array(res[m]) - SPHERE_ANALYTIC[m]) / np.array(SPHERE_ANALYTIC[m])
+        print("sphere mu*r", m, "max rel err vs analytic", err.max())
+
+
+if __name__ == "__main__":
+    main()

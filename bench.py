@@ -222,8 +222,12 @@ def run_ours(args):
     plan = tracer.Plan.from_sample(s)
     total_steps = plan.count_steps()
     grid, kernels = plan.launch_info()
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the legacy default stream has handle 0, which the
+    # library reads as "use the plan's own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
+    assert sh != 0
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         plan.run(sh)

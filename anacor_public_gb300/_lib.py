@@ -26,7 +26,7 @@ EXPORTS = (
     "anacor_plan_create", "anacor_plan_set_reflections", "anacor_plan_run", "anacor_plan_result",
     "anacor_plan_device_result", "anacor_plan_n_refl", "anacor_plan_launch_info", "anacor_plan_destroy",
     "anacor_plan_count_steps",
-    "anacor_batch_run", "anacor_rotated_vectors", "anacor_leg_detail",
+    "anacor_batch_run", "anacor_rotated_vectors", "anacor_leg_detail", "anacor_absorption_noalloc",
 )
 
 _LIB = None
@@ -115,6 +115,10 @@ def load(path: str | None = None) -> ct.CDLL:
     L.anacor_leg_detail.restype = ct.c_int
     L.anacor_leg_detail.argtypes = [_i8p, _i64p, _i64p, ct.c_int64, _f64p, _f64p, _f64p, ct.c_int,
                                     _i32p, _i32p, _i32p, _i32p, _i32p, _f64p, _i32p]
+    L.anacor_absorption_noalloc.restype = ct.c_int
+    L.anacor_absorption_noalloc.argtypes = [ct.c_void_p, _i64p, ct.c_void_p, ct.c_int64, _f64p, _f64p, ct.c_int64,
+                                            _f64p, _f64p, _f64p, _f64p, _f64p, ct.c_int, ct.c_int, ct.c_void_p,
+                                            ct.c_void_p]
     L.free.restype = None
     L.free.argtypes = [ct.c_void_p]
     if path == _build.LIB:

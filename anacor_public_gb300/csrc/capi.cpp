@@ -141,6 +141,14 @@ const int8_t *flat_base(int8_t ***table, const int64_t *shape)
 
 }  // namespace
 
+// Error reporting for entry points defined in other translation units.
+namespace anacor {
+int report_status(int st, const char *msg)
+{
+    return st ? fail(st, msg) : succeed();
+}
+}  // namespace anacor
+
 // ------------------------------------------------------------------ plans
 
 struct anacor_plan {

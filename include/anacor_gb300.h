@@ -132,6 +132,38 @@ void anacor_plan_destroy(anacor_plan *p);
  * own volumes, voxel lists and reflections).  Results land in each plan. */
 int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream);
 
+/* ------------------------------------------------- no-allocation entry -- */
+
+/* Size of the fixed device array behind anacor_absorption_noalloc.  Every GPU
+ * that loads the library holds it until the process exits. */
+#define ANACOR_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* No counterpart in the reference.  The absorption path for callers that must
+ * not allocate device memory: code that runs while someone else records a
+ * CUDA graph, hosts whose device memory belongs to a pool they do not
+ * control, pipelines that forbid allocation after start-up.  The caller
+ * passes device pointers for the C-contiguous int8 volume (d_label), the
+ * int64 (z, y, x) voxel list (d_coords) and the result array (d_out,
+ * n_refl doubles); s1, omega, xray, omega_axis, F, voxel, mu and shape are
+ * host arrays as for anacor_absorption.  Everything else -- packed voxels,
+ * reflection tables, tile partial sums, counters, the status word -- lives in
+ * one file-scope device array of ANACOR_NOALLOC_SCRATCH_BYTES bytes, so the
+ * call uses no cudaMalloc, cudaFree or other device allocator.  It needs
+ *   8*n_coords + n_refl*(868 + 8*ceil(n_coords/2048)) bytes + ~1 KiB;
+ * larger requests are rejected with ANACOR_ERR_ARGS (split the reflections
+ * over several calls).  The first call on a device looks up the array's
+ * address and uploads a constant table, so make that first call before any
+ * stream capture.  All calls share the one array and it keeps the previous
+ * call's contents: the call clears what must start at zero itself, and calls
+ * that overlap on the GPU (other streams, other threads) race on it.  Work is
+ * enqueued on `stream` (a cudaStream_t); the call returns after the stream
+ * has drained, with a status. */
+int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *shape, const int64_t *d_coords,
+                              int64_t n_coords, const double *s1, const double *omega, int64_t n_refl,
+                              const double *xray, const double *omega_axis, const double *F,
+                              const double *voxel, const double *mu, int full_iteration, int is_exp,
+                              double *d_out, void *stream);
+
 /* ---------------------------------------------------------- diagnostics -- */
 
 /* Rotated incident and diffracted vectors of n reflections, computed by the

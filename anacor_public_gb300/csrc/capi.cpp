@@ -61,6 +61,8 @@ struct DeviceState {
     int sms = 0;
     int blocks_per_sm = 0;
     cudaStream_t stream = nullptr;
+    double *qtab = nullptr;   // quotient table for den <= qtab_den (never freed: plans keep pointers)
+    int qtab_den = 0;
 };
 
 std::mutex g_mu;
@@ -110,6 +112,29 @@ void dev_free(T *&p, cudaStream_t st)
     if (p)
         cudaFreeAsync(p, st);
     p = nullptr;
+}
+
+// Quotient table covering den <= max_den on this device (nullptr when the
+// volume is larger than the table limit).
+const double *quotient_table(DeviceState *d, int max_den)
+{
+    if (max_den > kQuotientTableMaxDen)
+        return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (d->qtab_den < max_den) {
+        // grow in steps so that a series of plans does not rebuild it each time
+        const int den = std::min(kQuotientTableMaxDen, std::max(max_den, std::max(1025, 2 * d->qtab_den)));
+        double *q = nullptr;
+        if (cudaMalloc(&q, quotient_table_entries(den) * sizeof(double)) != cudaSuccess)
+            return nullptr;
+        if (launch_quotient_table(q, den, d->stream) != cudaSuccess || cudaStreamSynchronize(d->stream) != cudaSuccess) {
+            cudaFree(q);
+            return nullptr;
+        }
+        d->qtab = q;
+        d->qtab_den = den;
+    }
+    return d->qtab;
 }
 
 bool valid_shape(const int64_t *shape)
@@ -169,6 +194,9 @@ struct anacor_plan {
     unsigned long long *d_counter = nullptr;
     SampleDesc *d_desc = nullptr;
     unsigned long long *d_steps = nullptr;
+    double *d_sq = nullptr;        // [3][sq_stride] fl(fl(d * voxel_a)^2)
+    int sq_stride = 0;
+    const double *d_qtab = nullptr;  // device quotient table (owned by the device state)
     ReflTable *h_refl = nullptr;   // pinned staging
     int64_t n_refl = 0, refl_cap = 0;
     int tiles = 0;
@@ -189,14 +217,17 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_counter, st);
     dev_free(p->d_desc, st);
     dev_free(p->d_steps, st);
+    dev_free(p->d_sq, st);
     if (p->h_refl)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
     cudaStreamSynchronize(st);
 }
 
+// `morton`: pack the voxel list in Morton order (A_h does not depend on the
+// order); per-voxel outputs keep the caller's order instead.
 int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
-              const double *voxel, const double *mu, int full, int is_exp)
+              const double *voxel, const double *mu, int full, int is_exp, bool morton = true)
 {
     if (!label || !shape || !coords || !voxel || !mu)
         return fail(kErrArgs, "null argument");
@@ -232,10 +263,25 @@ int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const i
         return cuda_fail(e, "volume upload");
     if (n > 0) {
         if ((e = cudaMemcpyAsync(d_c64, coords, (size_t)n * 3 * sizeof(long long), cudaMemcpyHostToDevice, st)) ||
-            (e = launch_pack_coords(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)))
+            (e = morton ? launch_pack_coords_morton(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)
+                        : launch_pack_coords(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)))
             return cuda_fail(e, "coordinate upload");
     }
     dev_free(d_c64, st);
+    // squared axis lengths for cal_path2_plus's total, as the reference
+    // computes them: pow((last - first) * voxel, 2) == t * t, t = d * voxel
+    p->sq_stride = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
+    std::vector<double> sq((size_t)3 * p->sq_stride, 0.0);
+    for (int a = 0; a < 3; a++)
+        for (int d = 0; d < p->dims[a]; d++) {
+            const double t = (double)d * voxel[a];
+            sq[(size_t)a * p->sq_stride + d] = t * t;
+        }
+    if ((e = dev_alloc(&p->d_sq, sq.size(), st)) ||
+        (e = cudaMemcpyAsync(p->d_sq, sq.data(), sq.size() * sizeof(double), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaStreamSynchronize(st)))
+        return cuda_fail(e, "table upload");
+    p->d_qtab = quotient_table(dev, p->sq_stride);
     return kOk;
 }
 
@@ -289,6 +335,9 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     d.partial = p->d_partial;
     d.arrive = p->d_arrive;
     d.status = p->d_status;
+    d.sq = p->d_sq;
+    d.sq_stride = p->sq_stride;
+    d.qtab = p->d_qtab;
     d.work_begin = work_begin;
     return d;
 }
@@ -728,7 +777,7 @@ int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *
         return fail(st, status_text(st));
     static const double mu0[4] = {0, 0, 0, 0};
     anacor_plan p;
-    int st = plan_init(&p, label, shape, coords, n, voxel, mu0, full_iteration, 1);
+    int st = plan_init(&p, label, shape, coords, n, voxel, mu0, full_iteration, 1, false);
     ReflTable *d_tab = nullptr;
     double *d_vox = nullptr;
     int *d_i = nullptr;
@@ -740,8 +789,9 @@ int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *
             (e = dev_alloc(&d_i, m * 10, p.stream)) || (e = dev_alloc(&d_L, m * 4, p.stream)) ||
             (e = cudaMemcpyAsync(d_tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, p.stream)) ||
             (e = cudaMemcpyAsync(d_vox, voxel, 3 * sizeof(double), cudaMemcpyHostToDevice, p.stream)) ||
-            (e = launch_leg_detail(d_tab, p.d_vol, p.dims, p.d_coords, (int)n, d_vox, full_iteration, d_i,
-                                   d_i + m, d_i + 2 * m, d_i + 3 * m, d_i + 6 * m, d_L, d_i + 9 * m, p.stream)))
+            (e = launch_leg_detail(d_tab, p.d_vol, p.dims, p.d_coords, (int)n, d_vox, full_iteration, p.d_sq,
+                                   p.sq_stride, p.d_qtab, d_i, d_i + m, d_i + 2 * m, d_i + 3 * m, d_i + 6 * m, d_L,
+                                   d_i + 9 * m, p.stream)))
             st = cuda_fail(e, "leg detail");
     }
     if (!st && n > 0) {

@@ -2,52 +2,67 @@
 //
 // One CTA processes one work item = (sample, reflection, tile of kTile
 // consecutive coordinate-list voxels).  Thread k of the CTA takes voxels
-// tile*kTile + k + j*kBlock, so the 32 lanes of a warp march 32 adjacent
-// crystal voxels (np.where order: adjacent x) along the same two directions.
-// Their positions differ by the same integer offset at every increment, so the
-// label reads of a warp stay within one or a few 32-byte sectors.
+// tile*kTile + k + j*kBlock, so the 32 lanes of a warp hold 32 adjacent
+// crystal voxels (np.where order: adjacent x) and march them along the same
+// two directions.
 //
-// Per voxel (the body of AnACor/src/ray_tracing.c:199-278):
+// Per voxel (the body of AnACor/src/ray_tracing.c:199-278), per leg:
 //   exit face  (cube_face, ray_tracing_basic.c:69-186): FP32 estimate of the
 //              three candidate distances, exact FP64 division only when the
 //              two smallest are within 2^-20 relative.
-//   march      (cal_coord, :396-1460): 32.32 fixed-point positions with one
-//              64-bit add per axis and step; a step whose fraction lies within
-//              kAmbiguityMargin of a rounding boundary is recomputed with the
-//              reference's two-rounding FP64 expression.  Faces whose ratios
-//              are too large for fixed point march in FP64 throughout.
+//   march      (cal_coord, :396-1460), warp-cooperative: lanes leaving through
+//              the same face share its step rule and differ only by an integer
+//              start offset, so one lane per increment computes the 32.32
+//              fixed-point displacement and the warp broadcasts it; each lane
+//              loads its label at base + displacement, eight increments in
+//              flight, and checks four labels per packed word.  Increments
+//              whose fraction lies within kAmbiguityMargin of a rounding
+//              boundary are recomputed with the reference's FP64 expression.
+//              Lanes that may touch a volume wall, faces with ratios beyond
+//              fixed-point range and full_iteration march per lane in FP64.
 //   lengths    (cal_path2_plus, :1462-1552): FP64, same operation order; the
-//              per-segment quotient fl(span / (len-1)) comes from a correctly
-//              rounded reciprocal table and one FMA correction (exhaustively
-//              checked for every span <= len <= kMaxDim+1 by the test suite).
-//   rate       (cal_rate, :1554-1583): FP64 sum, exp in FP32 after an FP64
-//              range reduction; per-thread Neumaier sums, warp-shuffle TwoSum
-//              reduction, FP64 combination of the tile partials in a fixed
+//              per-segment quotient fl(span / (len-1)) comes from a table of
+//              correctly rounded quotients, or from a correctly rounded
+//              reciprocal and one FMA correction (exhaustively checked).
+//   rate       (cal_rate, :1554-1583): FP64 exponent, exp in FP32 after an
+//              FP64 range reduction; per-thread Neumaier sums, warp-shuffle
+//              TwoSum reduction, tile partials combined in FP64 in a fixed
 //              order (deterministic for any schedule).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+
+#include <cstdlib>
 
 #include "anacor_internal.h"
 #include "trace_launch.h"
 
 namespace anacor {
 
-__device__ double g_rcp[kMaxDim + 2];   // g_rcp[d] = fl(1 / d)
+// g_num_rcp[d] = {(double)d, fl(1 / d)}: the quotient's operands without an
+// integer-to-double conversion on the FP64 pipe
+__device__ double2 g_num_rcp[kMaxDim + 2];
 
 namespace {
 
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
+// CTAs per SM the absorption kernel's register budget is sized for: the
+// kernel is instantiated for 1..4 and one variant is chosen per process
+// (ANACOR_CTAS_PER_SM, default kDefaultMinBlocks).
+constexpr int kDefaultMinBlocks = 4;
+// Label loads a lane has in flight before checking them (divides 32).
+constexpr int kMarchBatch = 8;
+constexpr unsigned kAll = 0xffffffffu;
 
 struct Vol {
     const int8_t *p;
     int dz, dy, dx;
 };
 
-__device__ __forceinline__ int clampi(int v, int hi)
+__device__ __forceinline__ int pick3(int k, int z, int y, int x)
 {
-    return min(max(v, 0), hi - 1);
+    return k == 0 ? z : (k == 1 ? y : x);
 }
 
 // C's `int64_t n = floor(v)` / `round(v)`, then the reference's clamp.
@@ -77,15 +92,15 @@ __device__ __forceinline__ int exit_face(const LegHead &h, int cz, int cy, int c
     if (cy == 0 && h.e[1] != 0.0) return 4;
     if (cz == 0 && h.e[0] != 0.0) return 2;
     const uint32_t sb = h.sign_bits;
-    // one candidate per axis: numerator n_a, face f_a
-    int nx = (sb & 4u) ? v.dx - cx : cx;
-    int ny = (sb & 2u) ? v.dy - cy : cy;
-    int nz = (sb & 1u) ? v.dz - cz : cz;
+    // one candidate per axis: numerator n_a
+    const int nx = (sb & 4u) ? v.dx - cx : cx;
+    const int ny = (sb & 2u) ? v.dy - cy : cy;
+    const int nz = (sb & 1u) ? v.dz - cz : cz;
     const bool hx = (sb & (4u | 32u)) != 0, hy = (sb & (2u | 16u)) != 0, hz = (sb & (1u | 8u)) != 0;
     const float inf = __int_as_float(0x7f800000);
-    float tx = hx ? (float)nx * h.inv[2] : inf;
-    float ty = hy ? (float)ny * h.inv[1] : inf;
-    float tz = hz ? (float)nz * h.inv[0] : inf;
+    const float tx = hx ? (float)nx * h.inv[2] : inf;
+    const float ty = hy ? (float)ny * h.inv[1] : inf;
+    const float tz = hz ? (float)nz * h.inv[0] : inf;
     // argmin with ties to the earlier axis (x, y, z)
     int best = 2;
     float t1 = tx, t2;
@@ -94,9 +109,9 @@ __device__ __forceinline__ int exit_face(const LegHead &h, int cz, int cy, int c
     if ((sb & 64u) || !(t1 < inf && t2 > t1 * (1.0f + 0x1p-20f))) {
         // close call: the reference's FP64 quotients decide
         const double dinf = __longlong_as_double(0x7ff0000000000000ll);
-        double ex = hx ? __ddiv_rn((double)nx, fabs(h.e[2])) : dinf;
-        double ey = hy ? __ddiv_rn((double)ny, fabs(h.e[1])) : dinf;
-        double ez = hz ? __ddiv_rn((double)nz, fabs(h.e[0])) : dinf;
+        const double ex = hx ? __ddiv_rn((double)nx, fabs(h.e[2])) : dinf;
+        const double ey = hy ? __ddiv_rn((double)ny, fabs(h.e[1])) : dinf;
+        const double ez = hz ? __ddiv_rn((double)nz, fabs(h.e[0])) : dinf;
         best = 2;
         double b = ex;
         if (ey < b) { b = ey; best = 1; }
@@ -111,48 +126,57 @@ __device__ __forceinline__ int exit_face(const LegHead &h, int cz, int cy, int c
     return pos ? 3 : 2;
 }
 
-struct March {
-    int len, nseg, prev, vac;
-    int fz, fy, fx;     // first path point
-    int lz, ly, lx;     // last path point
-};
-
-// Segment sink: mode 0 records (class, start) in shared memory; mode 1
-// accumulates lengths directly (second pass, when a leg has more class
-// changes than the shared buffer holds).
-struct Sink {
-    uint16_t *seg;      // stride kBlock
-    // second-pass state
-    double tot, den, rcp;
-    double L0, L1, L2, L3;
-    int open_cls, open_pos;
-};
-
-__device__ __forceinline__ double span_quotient(int span, double den, double rcp)
+// fl(span / den): from the quotient table (row den holds span = 1 .. den+1)
+// or from rcp = fl(1/den) with one FMA-exact remainder and one correction.
+__device__ __forceinline__ double seg_quotient(const double *qtab, int den_i, int span, double den, double rcp)
 {
-    // fl(span / den) from rcp = fl(1/den): q0 = fl(span*rcp), one FMA-exact
-    // remainder and one correction step.
-    const double s = (double)span;
+    if (qtab)
+        return __ldg(qtab + ((den_i - 1) * (den_i + 2)) / 2 + (span - 1));
+    const double s = g_num_rcp[span].x;
     const double q0 = __dmul_rn(s, rcp);
     const double r = __fma_rn(-q0, den, s);
     return __fma_rn(r, rcp, q0);
 }
 
-__device__ __forceinline__ void add_class(int cls, double term, double &L0, double &L1, double &L2, double &L3)
+// L[cls-1] += term in segment order.  The first term of a class is stored
+// as is (0.0 + term == term for the non-negative terms of cal_path2_plus).
+__device__ __forceinline__ void add_class(int cls, double term, int &seen, double *L)
 {
     if (cls < 1 || cls > 4)
         return;
-    double cur = cls == 1 ? L0 : (cls == 2 ? L1 : (cls == 3 ? L2 : L3));
-    double nv = __dadd_rn(cur, term);
-    L0 = cls == 1 ? nv : L0;
-    L1 = cls == 2 ? nv : L1;
-    L2 = cls == 3 ? nv : L2;
-    L3 = cls == 4 ? nv : L3;
+    const int bit = 1 << cls;
+    double nv = term;
+    if (seen & bit) {
+        const double cur = cls == 1 ? L[0] : (cls == 2 ? L[1] : (cls == 3 ? L[2] : L[3]));
+        nv = __dadd_rn(cur, term);
+    }
+    seen |= bit;
+    L[0] = cls == 1 ? nv : L[0];
+    L[1] = cls == 2 ? nv : L[1];
+    L[2] = cls == 3 ? nv : L[2];
+    L[3] = cls == 4 ? nv : L[3];
 }
 
+// Per-leg march state.  Accepted path points are the increments 0..last_i
+// (the march never skips one), so len_path_2 = last_i + 1.
+struct March {
+    int last_i, nseg, prev, vac;
+};
+
+// Where class changes go: mode 0 records (class, start) in shared memory;
+// mode 1 (second pass, when a leg has more class changes than the shared
+// buffer holds) accumulates the lengths directly.
+struct Sink {
+    uint16_t *seg;      // stride kBlock
+    const double *qtab;
+    double tot, den, rcp;
+    int den_i;
+    double L[4];
+    int open_cls, open_pos, seen;
+};
+
 template <int kMode>
-__device__ __forceinline__ bool visit(March &m, Sink &sk, int i, int lab, int pz, int py, int px,
-                                      int full, int vac_limit)
+__device__ __forceinline__ bool visit(March &m, Sink &sk, int i, int lab, int full, int vac_limit)
 {
     if (!full) {
         if (lab == 0)
@@ -167,43 +191,92 @@ __device__ __forceinline__ bool visit(March &m, Sink &sk, int i, int lab, int pz
             if (m.nseg < kMaxSegments)
                 sk.seg[m.nseg * kBlock] = (uint16_t)((lab << 13) | i);
         } else {
-            const double q = span_quotient(i - sk.open_pos, sk.den, sk.rcp);
-            add_class(sk.open_cls, __dmul_rn(sk.tot, q), sk.L0, sk.L1, sk.L2, sk.L3);
+            const double q = seg_quotient(sk.qtab, sk.den_i, i - sk.open_pos, sk.den, sk.rcp);
+            add_class(sk.open_cls, __dmul_rn(sk.tot, q), sk.seen, sk.L);
             sk.open_cls = lab;
             sk.open_pos = i;
         }
         m.nseg++;
     }
-    m.len++;
+    m.last_i = i;
     m.prev = lab;
-    m.lz = pz; m.ly = py; m.lx = px;
     return true;
 }
 
-// March one leg (cal_coord).  Returns false if the start voxel stops it.
-template <int kMode>
-__device__ __forceinline__ void march(const FaceRule &R, int cz, int cy, int cx, int steps, const Vol &v,
-                                      int full, March &m, Sink &sk)
+// Geometry of one leg through one exit face in the face's own axis order:
+// s = the step axis (the reference's loop axis, ratio exactly +-1), a and b
+// the two other axes (32.32 fixed point).
+struct LegGeom {
+    int cs, ca, cb;          // start coordinates
+    int hs, ha, hb;          // dim - 1
+    int Ss, Sa, Sb;          // element strides
+    int ds;                  // step direction (+1 / -1)
+    int ia, ib;              // axis index (0 z, 1 y, 2 x) of a and b
+    long long Qa, Qb;
+    uint32_t Ma, Mb;         // ambiguity margins (0 for exact axes)
+    long long off;           // 2^31 for round mode
+};
+
+__device__ __forceinline__ void leg_geom(const FaceRule &R, int cz, int cy, int cx, const Vol &v, LegGeom &g)
 {
-    const int8_t *__restrict__ vol = v.p;
-    const int sy = v.dx, sz = v.dy * v.dx;
-    const bool rnd = R.use_round;
-    int pz, py, px;
+    const int s = R.count_axis;
+    const int a = s == 0 ? 1 : 0;
+    const int b = s == 2 ? 1 : 2;
+    g.ia = a; g.ib = b;
+    g.cs = pick3(s, cz, cy, cx); g.ca = pick3(a, cz, cy, cx); g.cb = pick3(b, cz, cy, cx);
+    g.hs = pick3(s, v.dz, v.dy, v.dx) - 1; g.ha = pick3(a, v.dz, v.dy, v.dx) - 1;
+    g.hb = pick3(b, v.dz, v.dy, v.dx) - 1;
+    const int sz = v.dy * v.dx, sy = v.dx;
+    g.Ss = pick3(s, sz, sy, 1); g.Sa = pick3(a, sz, sy, 1); g.Sb = pick3(b, sz, sy, 1);
+    g.ds = R.q[s] > 0.0 ? 1 : -1;
+    g.Qa = R.Q[a]; g.Qb = R.Q[b];
+    g.Ma = ((R.exact_mask >> a) & 1) ? 0u : kAmbiguityMargin;
+    g.Mb = ((R.exact_mask >> b) & 1) ? 0u : kAmbiguityMargin;
+    g.off = R.use_round ? 0x80000000ll : 0ll;
+}
+
+// Path point at increment i, (z, y, x).
+__device__ __forceinline__ void point_at(const FaceRule &R, const LegGeom &g, int i, int cz, int cy, int cx,
+                                         const Vol &v, int &pz, int &py, int &px)
+{
     if (R.fast) {
-        pz = cz; py = cy; px = cx;
+        const int ps = min(max(g.cs + i * g.ds, 0), g.hs);
+        const long long Ea = ((long long)g.ca << 32) + g.off + (long long)i * g.Qa;
+        const long long Eb = ((long long)g.cb << 32) + g.off + (long long)i * g.Qb;
+        int pa, pb;
+        if (((uint32_t)Ea + g.Ma < 2u * g.Ma) | ((uint32_t)Eb + g.Mb < 2u * g.Mb)) {
+            pa = exact_axis(g.ca, i, R.q[g.ia], R.use_round, g.ha + 1);
+            pb = exact_axis(g.cb, i, R.q[g.ib], R.use_round, g.hb + 1);
+        } else {
+            pa = min(max((int)(Ea >> 32), 0), g.ha);
+            pb = min(max((int)(Eb >> 32), 0), g.hb);
+        }
+        const int s = R.count_axis;
+        pz = s == 0 ? ps : pa;
+        py = s == 1 ? ps : (s == 0 ? pa : pb);
+        px = s == 2 ? ps : pb;
     } else {
-        pz = exact_axis(cz, 0, R.q[0], rnd, v.dz);
-        py = exact_axis(cy, 0, R.q[1], rnd, v.dy);
-        px = exact_axis(cx, 0, R.q[2], rnd, v.dx);
+        pz = exact_axis(cz, i, R.q[0], R.use_round, v.dz);
+        py = exact_axis(cy, i, R.q[1], R.use_round, v.dy);
+        px = exact_axis(cx, i, R.q[2], R.use_round, v.dx);
     }
-    m.len = 1; m.nseg = 1; m.vac = 0;
-    m.fz = pz; m.fy = py; m.fx = px;
-    m.lz = pz; m.ly = py; m.lx = px;
+}
+
+// Per-lane march (cal_coord) for the lanes the cooperative march does not
+// take: walls within reach, huge ratios, full_iteration; and the second pass.
+template <int kMode>
+__device__ __noinline__ void march_lane(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx, int steps,
+                                        const Vol &v, int full, March &m, Sink &sk)
+{
+    m.last_i = 0; m.nseg = 1; m.vac = 0;
     if (kMode == 0)
         sk.seg[0] = (uint16_t)(3 << 13);
     if (steps <= 0)
         return;
-    int lab = __ldg(vol + (pz * sz + py * sy + px));
+    const int sz = v.dy * v.dx, sy = v.dx;
+    int z, y, x;
+    point_at(R, g, 0, cz, cy, cx, v, z, y, x);
+    const int lab = __ldg(v.p + (z * sz + y * sy + x));
     if (!full) {
         if (lab == 0)
             return;
@@ -213,55 +286,22 @@ __device__ __forceinline__ void march(const FaceRule &R, int cz, int cy, int cx,
             return;
     }
     m.prev = lab;
-    if (R.fast) {
-        const long long off = rnd ? 0x80000000ll : 0ll;
-        long long E0 = ((long long)cz << 32) + off;
-        long long E1 = ((long long)cy << 32) + off;
-        long long E2 = ((long long)cx << 32) + off;
-        const long long Q0 = R.Q[0], Q1 = R.Q[1], Q2 = R.Q[2];
-        const uint32_t M0 = (R.exact_mask & 1) ? 0u : kAmbiguityMargin;
-        const uint32_t M1 = (R.exact_mask & 2) ? 0u : kAmbiguityMargin;
-        const uint32_t M2 = (R.exact_mask & 4) ? 0u : kAmbiguityMargin;
-        for (int i = 1; i < steps; i += 4) {
-            int qz[4], qy[4], qx[4], lb[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                E0 += Q0; E1 += Q1; E2 += Q2;
-                int z = (int)(E0 >> 32), y = (int)(E1 >> 32), x = (int)(E2 >> 32);
-                const bool amb = ((uint32_t)E0 + M0 < 2u * M0) | ((uint32_t)E1 + M1 < 2u * M1) |
-                                 ((uint32_t)E2 + M2 < 2u * M2);
-                if (amb) {
-                    z = exact_axis(cz, i + k, R.q[0], rnd, v.dz);
-                    y = exact_axis(cy, i + k, R.q[1], rnd, v.dy);
-                    x = exact_axis(cx, i + k, R.q[2], rnd, v.dx);
-                } else {
-                    z = clampi(z, v.dz); y = clampi(y, v.dy); x = clampi(x, v.dx);
-                }
-                qz[k] = z; qy[k] = y; qx[k] = x;
-            }
-            // every position is clamped inside the volume, so reading ahead of
-            // a vacuum stop or of `steps` is always in bounds
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                lb[k] = __ldg(vol + (qz[k] * sz + qy[k] * sy + qx[k]));
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                if (i + k >= steps)
-                    return;
-                if (!visit<kMode>(m, sk, i + k, lb[k], qz[k], qy[k], qx[k], full, R.vac_limit))
-                    return;
-            }
-        }
-    } else {
-        for (int i = 1; i < steps; i++) {
-            const int z = exact_axis(cz, i, R.q[0], rnd, v.dz);
-            const int y = exact_axis(cy, i, R.q[1], rnd, v.dy);
-            const int x = exact_axis(cx, i, R.q[2], rnd, v.dx);
-            const int l = __ldg(vol + (z * sz + y * sy + x));
-            if (!visit<kMode>(m, sk, i, l, z, y, x, full, R.vac_limit))
-                return;
-        }
+    for (int i = 1; i < steps; i++) {
+        point_at(R, g, i, cz, cy, cx, v, z, y, x);
+        if (!visit<kMode>(m, sk, i, __ldg(v.p + (z * sz + y * sy + x)), full, R.vac_limit))
+            return;
     }
+}
+
+// Label of increment `inc` from the reference's FP64 expression (an
+// increment whose fixed-point fraction lies near a rounding boundary).
+__device__ __noinline__ uint32_t exact_label(const FaceRule &G, const LegGeom &g, int ga, int gb, int inc, int ds,
+                                             int Ss, int Sa, int Sb, const int8_t *vol)
+{
+    const int pa = exact_axis(g.ca, inc, G.q[ga], G.use_round, g.ha + 1);
+    const int pb = exact_axis(g.cb, inc, G.q[gb], G.use_round, g.hb + 1);
+    const int ps = g.cs + inc * ds;
+    return (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(vol) + ps * Ss + pa * Sa + pb * Sb);
 }
 
 struct LegResult {
@@ -270,55 +310,229 @@ struct LegResult {
     int first[3], last[3];
 };
 
-// cube_face + cal_coord + cal_path2_plus for one leg.
+// fl(fl(d * v_axis)^2), from the sample's table when it has one
+__device__ __forceinline__ double sq_len(const double *sq, int stride, int axis, int d, double vox)
+{
+    if (sq)
+        return __ldg(sq + axis * stride + d);
+    const double t = __dmul_rn((double)d, vox);
+    return __dmul_rn(t, t);
+}
+
+// cube_face + cal_coord + cal_path2_plus for one leg.  Called by all 32 lanes
+// of a warp together (warp-synchronous); `valid` marks lanes that hold a voxel.
+//
+// Warp-cooperative march: lanes whose rays leave through the same face share
+// that face's step rule, and their 32.32 positions differ only in the integer
+// part (c * 2^32).  So the displacement of increment i -- and whether its
+// fraction is near a rounding boundary -- is the same for every lane of the
+// group: lane j computes it for increment i0 + j, the warp broadcasts it with
+// shuffles, and each lane only adds it to its own start address, loads the
+// label and checks it.  A lane joins the group only if no clamp can occur on
+// its increments (both end points at least one voxel inside the volume) and
+// the face has fixed-point ratios; other lanes, and full_iteration, use the
+// per-lane march.
+template <bool kDetail>
 __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
-                                          const Vol &v, int full, const double *voxel, uint16_t *seg,
+                                          bool valid, const Vol &v, int full, const double *voxel,
+                                          const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
                                           LegResult &out)
 {
+    const int lane = threadIdx.x & 31;
     out.L[0] = out.L[1] = out.L[2] = out.L[3] = 0.0;
     out.len = 1; out.nseg = 1; out.status = kOk;
-    out.first[0] = cz; out.first[1] = cy; out.first[2] = cx;
-    out.last[0] = cz; out.last[1] = cy; out.last[2] = cx;
-    const int face = exit_face(h, cz, cy, cx, v);
+    if (kDetail) {
+        out.first[0] = cz; out.first[1] = cy; out.first[2] = cx;
+        out.last[0] = cz; out.last[1] = cy; out.last[2] = cx;
+    }
+    const int face = valid ? exit_face(h, cz, cy, cx, v) : 0;
     out.face = face;
-    if (face == 0) {
+    bool need = valid;
+    if (valid && face == 0) {
         out.status = kErrNoFace;
-        return;
+        need = false;
     }
-    const FaceRule &R = rules[face - 1];
-    if (R.status) {
+    const FaceRule &R = rules[face > 0 ? face - 1 : 0];
+    if (need && R.status) {
         out.status = R.status;
-        return;
+        need = false;
     }
-    const int cc = R.count_axis == 0 ? cz : (R.count_axis == 1 ? cy : cx);
-    const int dd = R.count_axis == 0 ? v.dz : (R.count_axis == 1 ? v.dy : v.dx);
-    const int steps = R.count_kind == 0 ? cc + 1 : (R.count_kind == 1 ? dd - cc : dd - cc + 1);
+    int steps = 0;
+    LegGeom g;
+    leg_geom(R, cz, cy, cx, v, g);
+    if (need) {
+        const int cc = pick3(R.count_axis, cz, cy, cx);
+        const int dd = pick3(R.count_axis, v.dz, v.dy, v.dx);
+        steps = R.count_kind == 0 ? cc + 1 : (R.count_kind == 1 ? dd - cc : dd - cc + 1);
+    }
     March m;
+    m.last_i = 0; m.nseg = 1; m.vac = 0; m.prev = 0;
     Sink sk;
     sk.seg = seg;
-    march<0>(R, cz, cy, cx, steps, v, full, m, sk);
-    out.len = m.len; out.nseg = m.nseg;
-    out.first[0] = m.fz; out.first[1] = m.fy; out.first[2] = m.fx;
-    out.last[0] = m.lz; out.last[1] = m.ly; out.last[2] = m.lx;
-    if (m.len == 1)
+
+    // ---- cooperative eligibility and increment 0
+    bool coop = need && R.fast && !full && steps >= 1;
+    // the last increment of a count_kind 2 face clamps the step axis; it is
+    // taken separately after the cooperative part
+    const int steps_eff = R.count_kind == 2 ? steps - 1 : steps;
+    if (coop && steps_eff > 1) {
+        const long long ena = g.off + (long long)(steps_eff - 1) * g.Qa;
+        const long long enb = g.off + (long long)(steps_eff - 1) * g.Qb;
+        const int a1 = g.ca + (int)((g.off + g.Qa) >> 32), an = g.ca + (int)(ena >> 32);
+        const int b1 = g.cb + (int)((g.off + g.Qb) >> 32), bn = g.cb + (int)(enb >> 32);
+        coop = min(a1, an) >= 1 && max(a1, an) <= g.ha - 1 && min(b1, bn) >= 1 && max(b1, bn) <= g.hb - 1;
+    }
+    const int base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
+    bool stopped = false, live = false;
+    if (coop) {
+        seg[0] = (uint16_t)(3 << 13);
+        const int lab0 = __ldg(v.p + base);
+        if (lab0 == 0) {
+            stopped = true;
+        } else {
+            m.prev = lab0;
+            live = steps_eff > 1;
+        }
+    }
+
+    // ---- cooperative march, one exit-face group at a time
+    unsigned pend = __ballot_sync(kAll, coop);
+    while (pend) {
+        const int f = __shfl_sync(kAll, face, __ffs(pend) - 1);
+        const unsigned grp = __ballot_sync(kAll, coop && face == f);
+        pend &= ~grp;
+        const bool mine = (grp >> lane) & 1u;
+        const FaceRule &G = rules[f - 1];
+        const int gs = G.count_axis, ga = gs == 0 ? 1 : 0, gb = gs == 2 ? 1 : 2;
+        const int sz = v.dy * v.dx, sy = v.dx;
+        const int Ss = pick3(gs, sz, sy, 1), Sa = pick3(ga, sz, sy, 1), Sb = pick3(gb, sz, sy, 1);
+        const int ds = G.q[gs] > 0.0 ? 1 : -1;
+        const long long Qa = G.Q[ga], Qb = G.Q[gb];
+        const uint32_t Ma = ((G.exact_mask >> ga) & 1) ? 0u : kAmbiguityMargin;
+        const uint32_t Mb = ((G.exact_mask >> gb) & 1) ? 0u : kAmbiguityMargin;
+        const long long off = G.use_round ? 0x80000000ll : 0ll;
+        const int lim = mine ? steps_eff : 0;
+        const int gmax = __reduce_max_sync(kAll, lim);
+        const uint8_t *p = reinterpret_cast<const uint8_t *>(v.p) + base;
+        bool on = mine && live;
+        uint32_t prev4 = (uint32_t)(uint8_t)m.prev * 0x01010101u;
+        for (int i0 = 1; i0 < gmax; i0 += 32) {
+            if (!__any_sync(kAll, on))
+                break;
+            const int i = i0 + lane;
+            const long long ea = off + (long long)i * Qa, eb = off + (long long)i * Qb;
+            const bool amb = ((uint32_t)ea + Ma < 2u * Ma) | ((uint32_t)eb + Mb < 2u * Mb);
+            const int delta = i * ds * Ss + (int)(ea >> 32) * Sa + (int)(eb >> 32) * Sb;
+            const unsigned ambm = __ballot_sync(kAll, amb);
+#pragma unroll 1
+            for (int t = 0; t < 32; t += kMarchBatch) {
+                if (!__any_sync(kAll, on))
+                    break;
+                const int ib = i0 + t;
+                uint32_t lb[kMarchBatch];
+#pragma unroll
+                for (int k = 0; k < kMarchBatch; k++) {
+                    const int dk = __shfl_sync(kAll, delta, t + k);
+                    lb[k] = (on && ib + k < lim) ? (uint32_t)__ldg(p + dk) : 0u;
+                }
+                const unsigned amb_here = (ambm >> t) & ((1u << kMarchBatch) - 1u);
+                if (amb_here) {
+                    // the reference's FP64 expression decides, per lane (c enters its rounding)
+                    for (int k = 0; k < kMarchBatch; k++)
+                        if (((amb_here >> k) & 1u) && on && ib + k < lim)
+                            lb[k] = exact_label(G, g, ga, gb, ib + k, ds, Ss, Sa, Sb, v.p);
+                }
+                if (on) {
+                    // Four increments per packed word; the bytes that are zero
+                    // (stop) or differ from the previous label (class change)
+                    // are found with SIMD byte compares and handled one event
+                    // at a time, in increment order.
+                    const int n = lim - ib;
+#pragma unroll
+                    for (int q = 0; q < kMarchBatch / 4; q++) {
+                        const int b4 = ib + 4 * q;
+                        const int nq = n - 4 * q;
+                        if (!stopped && nq > 0) {
+                            const uint32_t w = lb[4 * q] | (lb[4 * q + 1] << 8) | (lb[4 * q + 2] << 16) |
+                                               (lb[4 * q + 3] << 24);
+                            const uint32_t valid_bytes = nq >= 4 ? 0xffffffffu : (1u << (8 * nq)) - 1u;
+                            uint32_t ev = (__vcmpne4(w, prev4) | __vcmpeq4(w, 0u)) & valid_bytes;
+                            while (ev) {
+                                const int byte = (__ffs(ev) - 1) >> 3;
+                                const int lab = (int)(signed char)(w >> (8 * byte));
+                                const int inc = b4 + byte;
+                                if (lab == 0) {
+                                    stopped = true;
+                                    m.last_i = inc - 1;
+                                    break;
+                                }
+                                if ((unsigned)lab <= 4u) {
+                                    if (m.nseg < kMaxSegments)
+                                        seg[m.nseg * kBlock] = (uint16_t)((lab << 13) | inc);
+                                    m.nseg++;
+                                }
+                                m.prev = lab;
+                                prev4 = (uint32_t)(uint8_t)lab * 0x01010101u;
+                                ev = (__vcmpne4(w, prev4) | __vcmpeq4(w, 0u)) & valid_bytes &
+                                     (byte == 3 ? 0u : (0xffffffffu << (8 * (byte + 1))));
+                            }
+                            if (!stopped)
+                                m.last_i = b4 + min(nq, 4) - 1;
+                        }
+                    }
+                    if (stopped || ib + kMarchBatch >= lim)
+                        on = false;
+                }
+            }
+        }
+    }
+    if (coop && !stopped && steps_eff < steps) {
+        // the clamped last increment of a count_kind 2 face
+        int pz, py, px;
+        const int inc = steps - 1;
+        point_at(R, g, inc, cz, cy, cx, v, pz, py, px);
+        const int lab = __ldg(v.p + (pz * v.dy * v.dx + py * v.dx + px));
+        if (inc >= 1)
+            visit<0>(m, sk, inc, lab, 0, R.vac_limit);
+    }
+    if (need && !coop)
+        march_lane<0>(R, g, cz, cy, cx, steps, v, full, m, sk);
+    if (!need)
         return;
+
+    // ---- cal_path2_plus
+    const int len = m.last_i + 1;
+    out.len = len;
+    out.nseg = m.nseg;
+    if (len == 1 && !kDetail)
+        return;
+    int fz = cz, fy = cy, fx = cx;
+    if (!R.fast)
+        point_at(R, g, 0, cz, cy, cx, v, fz, fy, fx);
+    int lz, ly, lx;
+    point_at(R, g, m.last_i, cz, cy, cx, v, lz, ly, lx);
+    if (kDetail) {
+        out.first[0] = fz; out.first[1] = fy; out.first[2] = fx;
+        out.last[0] = lz; out.last[1] = ly; out.last[2] = lx;
+        if (len == 1)
+            return;
+    }
     // total from the first and last path points, y then z then x
-    const double dy = __dmul_rn((double)(m.ly - m.fy), voxel[1]);
-    const double dz = __dmul_rn((double)(m.lz - m.fz), voxel[0]);
-    const double dx = __dmul_rn((double)(m.lx - m.fx), voxel[2]);
-    const double tot = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dz, dz)), __dmul_rn(dx, dx)));
-    const int den_i = m.len - 1;
-    const double den = (double)den_i;
-    const double rcp = g_rcp[den_i];
-    double L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
+    const double yy = sq_len(sq, sq_stride, 1, abs(ly - fy), voxel[1]);
+    const double zz = sq_len(sq, sq_stride, 0, abs(lz - fz), voxel[0]);
+    const double xx = sq_len(sq, sq_stride, 2, abs(lx - fx), voxel[2]);
+    const double tot = __dsqrt_rn(__dadd_rn(__dadd_rn(yy, zz), xx));
+    const int den_i = len - 1;
+    const double2 dr = g_num_rcp[den_i];
+    int seen = 0;
     if (m.nseg <= kMaxSegments) {
         int cur = seg[0];
         for (int j = 0; j < m.nseg; j++) {
             const int nxt = (j + 1 < m.nseg) ? (int)seg[(j + 1) * kBlock] : -1;
             const int start = cur & 0x1fff;
-            const int end = (j + 1 < m.nseg) ? (nxt & 0x1fff) : m.len;
-            const double q = span_quotient(end - start, den, rcp);
-            add_class(cur >> 13, __dmul_rn(tot, q), L0, L1, L2, L3);
+            const int end = (j + 1 < m.nseg) ? (nxt & 0x1fff) : len;
+            const double q = seg_quotient(qtab, den_i, end - start, dr.x, dr.y);
+            add_class(cur >> 13, __dmul_rn(tot, q), seen, out.L);
             cur = nxt;
         }
     } else {
@@ -327,25 +541,16 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         March m2;
         Sink s2;
         s2.seg = seg;
-        s2.tot = tot; s2.den = den; s2.rcp = rcp;
-        s2.L0 = s2.L1 = s2.L2 = s2.L3 = 0.0;
-        s2.open_cls = 3; s2.open_pos = 0;
-        march<1>(R, cz, cy, cx, steps, v, full, m2, s2);
-        const double q = span_quotient(m.len - s2.open_pos, den, rcp);
-        add_class(s2.open_cls, __dmul_rn(tot, q), s2.L0, s2.L1, s2.L2, s2.L3);
-        L0 = s2.L0; L1 = s2.L1; L2 = s2.L2; L3 = s2.L3;
+        s2.qtab = qtab;
+        s2.tot = tot; s2.den = dr.x; s2.rcp = dr.y; s2.den_i = den_i;
+        s2.L[0] = s2.L[1] = s2.L[2] = s2.L[3] = 0.0;
+        s2.open_cls = 3; s2.open_pos = 0; s2.seen = 0;
+        march_lane<1>(R, g, cz, cy, cx, steps, v, full, m2, s2);
+        const double q = seg_quotient(qtab, den_i, len - s2.open_pos, dr.x, dr.y);
+        add_class(s2.open_cls, __dmul_rn(tot, q), s2.seen, s2.L);
+        for (int k = 0; k < 4; k++)
+            out.L[k] = s2.L[k];
     }
-    out.L[0] = L0; out.L[1] = L1; out.L[2] = L2; out.L[3] = L3;
-}
-
-// cal_rate's exponent, operand order of AnACor/src/ray_tracing_basic.c:1573-1576
-__device__ __forceinline__ double rate_exponent(const double *mu, const double *a, const double *b)
-{
-    const double t0 = __dmul_rn(mu[0], __dadd_rn(a[0], b[0]));
-    const double t1 = __dmul_rn(mu[1], __dadd_rn(a[1], b[1]));
-    const double t2 = __dmul_rn(mu[2], __dadd_rn(a[2], b[2]));
-    const double t3 = __dmul_rn(mu[3], __dadd_rn(a[3], b[3]));
-    return __dadd_rn(__dadd_rn(__dadd_rn(t0, t1), t2), t3);
 }
 
 // exp(-x) in FP32 after an FP64 reduction x = k ln2 + r, |r| <= ln2/2.
@@ -373,9 +578,10 @@ __device__ __forceinline__ int find_sample(const SampleDesc *d, int n, long long
     return s;
 }
 
-__global__ void __launch_bounds__(kBlock) absorption_kernel(const SampleDesc *__restrict__ descs, int n_desc,
-                                                            long long total_items,
-                                                            unsigned long long *__restrict__ work_counter)
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const SampleDesc *__restrict__ descs,
+                                                                        int n_desc, long long total_items,
+                                                                        unsigned long long *__restrict__ work_counter)
 {
     __shared__ ReflTable tab;
     __shared__ uint16_t seg[kMaxSegments * kBlock];
@@ -410,19 +616,41 @@ __global__ void __launch_bounds__(kBlock) absorption_kernel(const SampleDesc *__
         unsigned nsteps = 0;
         const int v0 = t * kTile;
         const int v1 = min(D.n_vox, v0 + kTile);
-        for (int vi = v0 + tid; vi < v1; vi += kBlock) {
-            const short4 cv = __ldg(D.coords + vi);
-            LegResult a, b;
-            trace_leg(tab.head[0], tab.rule[0], cv.x, cv.y, cv.z, v, D.full_iteration, D.voxel, seg + tid, a);
-            trace_leg(tab.head[1], tab.rule[1], cv.x, cv.y, cv.z, v, D.full_iteration, D.voxel, seg + tid, b);
-            bad |= a.status | b.status;
-            nsteps += (unsigned)(a.len + b.len);
-            const double ex = rate_exponent(D.mu, a.L, b.L);
-            const float term = D.is_exp ? exp_neg(ex) : (float)ex;
-            float ns, e;
-            two_sum(s, term, ns, e);
-            s = ns;
-            c += e;
+        // every lane runs the same number of iterations (the march is warp-synchronous)
+        for (int vb = v0; vb < v1; vb += kBlock) {
+            const int vi = vb + tid;
+            const bool valid = vi < v1;
+            const short4 cv = valid ? __ldg(D.coords + vi) : make_short4(0, 0, 0, 0);
+            double Ls[4];
+#pragma unroll 1
+            for (int leg = 0; leg < 2; leg++) {
+                LegResult a;
+                trace_leg<false>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v, D.full_iteration,
+                                 D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
+                bad |= a.status;
+                nsteps += valid ? (unsigned)a.len : 0u;
+                if (leg == 0) {
+                    for (int k = 0; k < 4; k++)
+                        Ls[k] = a.L[k];
+                } else {
+                    // (L_incident + L_diffracted) per class, as cal_rate adds them
+                    for (int k = 0; k < 4; k++)
+                        Ls[k] = __dadd_rn(Ls[k], a.L[k]);
+                }
+            }
+            if (valid) {
+                // cal_rate's exponent, operand order of AnACor/src/ray_tracing_basic.c:1573-1576
+                const double t0 = __dmul_rn(D.mu[0], Ls[0]);
+                const double t1 = __dmul_rn(D.mu[1], Ls[1]);
+                const double t2 = __dmul_rn(D.mu[2], Ls[2]);
+                const double t3 = __dmul_rn(D.mu[3], Ls[3]);
+                const double ex = __dadd_rn(__dadd_rn(__dadd_rn(t0, t1), t2), t3);
+                const float term = D.is_exp ? exp_neg(ex) : (float)ex;
+                float ns, e;
+                two_sum(s, term, ns, e);
+                s = ns;
+                c += e;
+            }
         }
         if (bad)
             atomicOr(D.status, 1 << bad);
@@ -430,15 +658,15 @@ __global__ void __launch_bounds__(kBlock) absorption_kernel(const SampleDesc *__
             unsigned long long w = nsteps;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1)
-                w += __shfl_down_sync(0xffffffffu, w, o);
+                w += __shfl_down_sync(kAll, w, o);
             if (lane == 0)
                 atomicAdd(D.steps, w);
         }
         // warp-shuffle TwoSum reduction of (s, c)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const float so = __shfl_down_sync(0xffffffffu, s, o);
-            const float co = __shfl_down_sync(0xffffffffu, c, o);
+            const float so = __shfl_down_sync(kAll, s, o);
+            const float co = __shfl_down_sync(kAll, c, o);
             float ns, e;
             two_sum(s, so, ns, e);
             s = ns;
@@ -466,13 +694,13 @@ __global__ void __launch_bounds__(kBlock) absorption_kernel(const SampleDesc *__
         if (last_s && warp == 0) {
             // the last tile of this reflection combines all partials in a fixed order
             __threadfence();
-            const volatile double *p = D.partial + r * D.tiles;
+            const volatile double *pp = D.partial + r * D.tiles;
             double acc = 0.0;
             for (int k = lane; k < D.tiles; k += 32)
-                acc += p[k];
+                acc += pp[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1)
-                acc += __shfl_down_sync(0xffffffffu, acc, o);
+                acc += __shfl_down_sync(kAll, acc, o);
             if (lane == 0) {
                 D.out[r] = acc / (double)D.n_vox;
                 D.arrive[r] = 0u;   // ready for the next launch
@@ -481,11 +709,14 @@ __global__ void __launch_bounds__(kBlock) absorption_kernel(const SampleDesc *__
     }
 }
 
-// Per-voxel, per-leg detail for one reflection (path-level parity checks).
+// Per-voxel, per-leg detail for one reflection (path-level parity checks);
+// same march code as the absorption kernel.
 __global__ void __launch_bounds__(kBlock) leg_detail_kernel(const ReflTable *__restrict__ tabp, const int8_t *vol,
                                                             int dz, int dy, int dx, const short4 *coords, int n,
-                                                            const double *voxel3, int full, int *face, int *len,
-                                                            int *nseg, int *first, int *last, double *L, int *status)
+                                                            const double *voxel3, int full, const double *sq,
+                                                            int sq_stride, const double *qtab, int *face, int *len,
+                                                            int *nseg, int *first, int *last, double *L,
+                                                            int *status)
 {
     __shared__ ReflTable tab;
     __shared__ uint16_t seg[kMaxSegments * kBlock];
@@ -500,13 +731,16 @@ __global__ void __launch_bounds__(kBlock) leg_detail_kernel(const ReflTable *__r
     }
     __syncthreads();
     const int vi = blockIdx.x * kBlock + threadIdx.x;
-    if (vi >= n)
-        return;
+    const bool valid = vi < n;
     const Vol v{vol, dz, dy, dx};
-    const short4 cv = coords[vi];
+    const short4 cv = valid ? coords[vi] : make_short4(0, 0, 0, 0);
+#pragma unroll 1
     for (int leg = 0; leg < 2; leg++) {
         LegResult a;
-        trace_leg(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, v, full, vox, seg + threadIdx.x, a);
+        trace_leg<true>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v, full, vox, sq, sq_stride, qtab,
+                        seg + threadIdx.x, a);
+        if (!valid)
+            continue;
         const int o = 2 * vi + leg;
         face[o] = a.face;
         len[o] = a.len;
@@ -537,15 +771,48 @@ __global__ void pack_coords_kernel(const long long *__restrict__ c, int n, int d
     out[i] = make_short4((short)z, (short)y, (short)x, 0);
 }
 
+// Quotient table: row d (1 <= d <= max_den) holds fl(s / d) for s = 1 .. d+1,
+// rows packed one after another (row d starts at (d-1)(d+2)/2).
+__global__ void quotient_table_kernel(double *__restrict__ q, int max_den)
+{
+    const long long total = (long long)max_den * (max_den + 3) / 2;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        // row d: the largest d with (d-1)(d+2)/2 <= k
+        int d = (int)floor((sqrt(8.0 * (double)k + 9.0) - 1.0) / 2.0);
+        if (d < 1)
+            d = 1;
+        while (d > 1 && (long long)(d - 1) * (d + 2) / 2 > k)
+            d--;
+        while ((long long)d * (d + 3) / 2 <= k)
+            d++;
+        const int s = (int)(k - (long long)(d - 1) * (d + 2) / 2) + 1;
+        q[k] = __ddiv_rn((double)s, (double)d);
+    }
+}
+
 }  // namespace
 
 int rcp_table_init()
 {
-    static double host[kMaxDim + 2];
-    host[0] = 0.0;
+    static double2 host[kMaxDim + 2];
+    host[0] = make_double2(0.0, 0.0);
     for (int d = 1; d < kMaxDim + 2; d++)
-        host[d] = 1.0 / (double)d;
-    return cudaMemcpyToSymbol(g_rcp, host, sizeof(host)) == cudaSuccess ? kOk : kErrCuda;
+        host[d] = make_double2((double)d, 1.0 / (double)d);
+    return cudaMemcpyToSymbol(g_num_rcp, host, sizeof(host)) == cudaSuccess ? kOk : kErrCuda;
+}
+
+size_t quotient_table_entries(int max_den)
+{
+    return max_den > 0 ? (size_t)max_den * (size_t)(max_den + 3) / 2 : 0;
+}
+
+cudaError_t launch_quotient_table(double *d_q, int max_den, cudaStream_t st)
+{
+    if (max_den <= 0)
+        return cudaSuccess;
+    quotient_table_kernel<<<1024, 256, 0, st>>>(d_q, max_den);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_pack_coords(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
@@ -557,6 +824,16 @@ cudaError_t launch_pack_coords(const long long *d_c, int n, const int *dims, sho
     return cudaGetLastError();
 }
 
+int absorption_variant()
+{
+    static const int v = [] {
+        const char *e = std::getenv("ANACOR_CTAS_PER_SM");
+        const int x = e ? std::atoi(e) : kDefaultMinBlocks;
+        return (x >= 1 && x <= 4) ? x : kDefaultMinBlocks;
+    }();
+    return v;
+}
+
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,
                               unsigned long long *d_counter, int grid, cudaStream_t st)
 {
@@ -565,19 +842,25 @@ cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long t
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess)
         return e;
-    absorption_kernel<<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter);
+    switch (absorption_variant()) {
+    case 1: absorption_kernel<1><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
+    case 3: absorption_kernel<3><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
+    case 4: absorption_kernel<4><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
+    default: absorption_kernel<2><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const int *dims, const short4 *d_coords,
-                              int n, const double *d_voxel, int full, int *face, int *len, int *nseg, int *first,
-                              int *last, double *L, int *status, cudaStream_t st)
+                              int n, const double *d_voxel, int full, const double *d_sq, int sq_stride,
+                              const double *d_qtab, int *face, int *len, int *nseg, int *first, int *last, double *L,
+                              int *status, cudaStream_t st)
 {
     if (n <= 0)
         return cudaSuccess;
     leg_detail_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(d_tab, d_vol, dims[0], dims[1], dims[2],
-                                                                    d_coords, n, d_voxel, full, face, len, nseg,
-                                                                    first, last, L, status);
+                                                                    d_coords, n, d_voxel, full, d_sq, sq_stride,
+                                                                    d_qtab, face, len, nseg, first, last, L, status);
     return cudaGetLastError();
 }
 
@@ -585,10 +868,14 @@ int absorption_block_threads() { return kBlock; }
 
 int absorption_occupancy(int *blocks_per_sm)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel, kBlock, 0) ==
-                   cudaSuccess
-               ? kOk
-               : kErrCuda;
+    cudaError_t e;
+    switch (absorption_variant()) {
+    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<1>, kBlock, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<3>, kBlock, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<4>, kBlock, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<2>, kBlock, 0); break;
+    }
+    return e == cudaSuccess ? kOk : kErrCuda;
 }
 
 }  // namespace anacor

@@ -27,6 +27,9 @@ EXPORTS = (
     "anacor_plan_device_result", "anacor_plan_n_refl", "anacor_plan_launch_info", "anacor_plan_destroy",
     "anacor_plan_count_steps",
     "anacor_batch_run", "anacor_rotated_vectors", "anacor_leg_detail", "anacor_absorption_noalloc",
+    "anacor_plan_configure", "anacor_plan_config", "anacor_plan_autotune", "anacor_batch_create",
+    "anacor_batch_configure", "anacor_batch_autotune", "anacor_batch_launch", "anacor_batch_capture",
+    "anacor_batch_replay", "anacor_batch_wait", "anacor_batch_info", "anacor_batch_destroy",
 )
 
 _LIB = None
@@ -119,6 +122,26 @@ def load(path: str | None = None) -> ct.CDLL:
     L.anacor_absorption_noalloc.argtypes = [ct.c_void_p, _i64p, ct.c_void_p, ct.c_int64, _f64p, _f64p, ct.c_int64,
                                             _f64p, _f64p, _f64p, _f64p, _f64p, ct.c_int, ct.c_int, ct.c_void_p,
                                             ct.c_void_p]
+    L.anacor_plan_configure.restype = ct.c_int
+    L.anacor_plan_configure.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int]
+    L.anacor_plan_config.restype = ct.c_int
+    L.anacor_plan_config.argtypes = [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]
+    L.anacor_plan_autotune.restype = ct.c_int
+    L.anacor_plan_autotune.argtypes = [ct.c_void_p, ct.c_int64, ct.POINTER(ct.c_float)]
+    L.anacor_batch_create.restype = ct.c_void_p
+    L.anacor_batch_create.argtypes = [ct.POINTER(ct.c_void_p), ct.c_int]
+    for name in ("anacor_batch_launch", "anacor_batch_capture", "anacor_batch_replay", "anacor_batch_wait"):
+        getattr(L, name).restype = ct.c_int
+        getattr(L, name).argtypes = [ct.c_void_p, ct.c_void_p]
+    L.anacor_batch_configure.restype = ct.c_int
+    L.anacor_batch_configure.argtypes = [ct.c_void_p, ct.c_int]
+    L.anacor_batch_autotune.restype = ct.c_int
+    L.anacor_batch_autotune.argtypes = [ct.c_void_p, ct.c_int64]
+    L.anacor_batch_info.restype = ct.c_int
+    L.anacor_batch_info.argtypes = [ct.c_void_p, ct.POINTER(ct.c_int), ct.POINTER(ct.c_longlong),
+                                    ct.POINTER(ct.c_int)]
+    L.anacor_batch_destroy.restype = None
+    L.anacor_batch_destroy.argtypes = [ct.c_void_p]
     L.free.restype = None
     L.free.argtypes = [ct.c_void_p]
     if path == _build.LIB:

@@ -9,7 +9,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -63,10 +65,27 @@ struct DeviceState {
     cudaStream_t stream = nullptr;
     double *qtab = nullptr;   // quotient table for den <= qtab_den (never freed: plans keep pointers)
     int qtab_den = 0;
+    int bps[5] = {0, 0, 0, 0, 0};   // CTAs per SM of each register-budget variant (index 1..4)
 };
+
 
 std::mutex g_mu;
 DeviceState g_dev[64];
+
+// CTAs per SM of `variant` (0: the process default) on this device
+int variant_occupancy(DeviceState *d, int variant)
+{
+    const int v = variant > 0 ? variant : absorption_variant();
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!d->bps[v]) {
+        int b = 0;
+        if (absorption_occupancy(&b, v) != kOk || b <= 0)
+            b = 1;
+        d->bps[v] = b;
+    }
+    return d->bps[v];
+}
+
 
 int current_device(DeviceState **out)
 {
@@ -200,6 +219,10 @@ struct anacor_plan {
     ReflTable *h_refl = nullptr;   // pinned staging
     int64_t n_refl = 0, refl_cap = 0;
     int tiles = 0;
+    int tile = kTile;              // voxels per work item
+    int variant = 0;               // register-budget variant (0: process default)
+    bool morton = true;            // voxel list packed in Morton order
+    long long *d_c64 = nullptr;    // the caller's int64 voxel list (for re-packing)
 };
 
 namespace {
@@ -218,6 +241,7 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_desc, st);
     dev_free(p->d_steps, st);
     dev_free(p->d_sq, st);
+    dev_free(p->d_c64, st);
     if (p->h_refl)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
@@ -249,15 +273,17 @@ int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const i
     p->n_vox = (int)n;
     p->full = full;
     p->is_exp = is_exp;
+    p->morton = morton;
+    p->tile = kTile;
     p->tiles = (int)((n + kTile - 1) / kTile);
     cudaStream_t st = p->stream;
     const size_t nvol = (size_t)shape[0] * shape[1] * shape[2];
     cudaError_t e;
-    long long *d_c64 = nullptr;
     if ((e = dev_alloc(&p->d_vol, nvol, st)) != cudaSuccess || (e = dev_alloc(&p->d_coords, (size_t)n, st)) ||
         (e = dev_alloc(&p->d_status, 1, st)) || (e = dev_alloc(&p->d_counter, 1, st)) ||
-        (e = dev_alloc(&p->d_desc, 1, st)) || (e = dev_alloc(&d_c64, (size_t)n * 3, st)))
+        (e = dev_alloc(&p->d_desc, 1, st)) || (e = dev_alloc(&p->d_c64, (size_t)n * 3, st)))
         return cuda_fail(e, "device allocation");
+    long long *d_c64 = p->d_c64;
     if ((e = cudaMemcpyAsync(p->d_vol, label, nvol, cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemsetAsync(p->d_status, 0, sizeof(int), st)))
         return cuda_fail(e, "volume upload");
@@ -267,7 +293,6 @@ int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const i
                         : launch_pack_coords(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)))
             return cuda_fail(e, "coordinate upload");
     }
-    dev_free(d_c64, st);
     // squared axis lengths for cal_path2_plus's total, as the reference
     // computes them: pow((last - first) * voxel, 2) == t * t, t = d * voxel
     p->sq_stride = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
@@ -300,7 +325,8 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
             p->h_refl = nullptr;
         }
         if ((e = dev_alloc(&p->d_refl, (size_t)n_refl, st)) || (e = dev_alloc(&p->d_out, (size_t)n_refl, st)) ||
-            (e = dev_alloc(&p->d_partial, (size_t)n_refl * (size_t)std::max(p->tiles, 1), st)) ||
+            (e = dev_alloc(&p->d_partial,
+                           (size_t)n_refl * (size_t)std::max(1, (p->n_vox + kMinTile - 1) / kMinTile), st)) ||
             (e = dev_alloc(&p->d_arrive, (size_t)n_refl, st)))
             return cuda_fail(e, "device allocation");
         if ((e = cudaMemsetAsync(p->d_arrive, 0, (size_t)n_refl * sizeof(unsigned), st)))
@@ -329,6 +355,7 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     d.refl = p->d_refl;
     d.n_refl = p->n_refl;
     d.tiles = p->tiles;
+    d.tile = p->tile;
     d.full_iteration = p->full;
     d.is_exp = p->is_exp;
     d.out = p->d_out;
@@ -366,10 +393,15 @@ int plan_upload_tables(anacor_plan *p)
     return plan_upload_desc(p, nullptr);
 }
 
+int grid_for(DeviceState *d, int variant, long long items)
+{
+    const long long cap = (long long)d->sms * variant_occupancy(d, variant);
+    return (int)std::max(1ll, std::min(items, cap));
+}
+
 int plan_grid(const anacor_plan *p, long long items)
 {
-    const long long cap = (long long)p->dev->sms * p->dev->blocks_per_sm;
-    return (int)std::max(1ll, std::min(items, cap));
+    return grid_for(p->dev, p->variant, items);
 }
 
 int plan_launch(anacor_plan *p, cudaStream_t st)
@@ -377,7 +409,7 @@ int plan_launch(anacor_plan *p, cudaStream_t st)
     const long long items = (long long)p->n_refl * p->tiles;
     if (items == 0)
         return kOk;
-    cudaError_t e = launch_absorption(p->d_desc, 1, items, p->d_counter, plan_grid(p, items), st);
+    cudaError_t e = launch_absorption(p->d_desc, 1, items, p->d_counter, plan_grid(p, items), st, p->variant);
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return kOk;
@@ -432,6 +464,131 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     t_status = keep;
     t_msg = msg;
     return st;
+}
+
+
+int plan_configure(anacor_plan *p, int variant, int tile, int morton)
+{
+    if (variant < 0 || variant > 4 || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) || morton < -1 ||
+        morton > 1)
+        return fail(kErrArgs, "bad plan configuration");
+    cudaError_t e;
+    if (morton >= 0 && (morton != 0) != p->morton && p->n_vox > 0) {
+        e = morton ? launch_pack_coords_morton(p->d_c64, p->n_vox, p->dims, p->d_coords, p->d_status, p->stream)
+                   : launch_pack_coords(p->d_c64, p->n_vox, p->dims, p->d_coords, p->d_status, p->stream);
+        if (e)
+            return cuda_fail(e, "voxel list packing");
+        p->morton = morton != 0;
+    }
+    if (tile) {
+        p->tile = tile;
+        p->tiles = (int)(((long long)p->n_vox + tile - 1) / tile);
+    }
+    p->variant = variant;
+    return plan_upload_desc(p, nullptr);
+}
+
+// Time `reps` launches over the first k reflections of the plan (ms each).
+int plan_time(anacor_plan *p, int64_t k, int reps, float *ms)
+{
+    const int64_t keep = p->n_refl;
+    p->n_refl = k;
+    int st = plan_upload_desc(p, nullptr);
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!st && ((e = cudaEventCreate(&a)) || (e = cudaEventCreate(&b))))
+        st = cuda_fail(e, "event");
+    if (!st)
+        st = plan_launch(p, p->stream);   // warm-up
+    if (!st && (e = cudaEventRecord(a, p->stream)))
+        st = cuda_fail(e, "event");
+    for (int r = 0; !st && r < reps; r++)
+        st = plan_launch(p, p->stream);
+    if (!st && ((e = cudaEventRecord(b, p->stream)) || (e = cudaEventSynchronize(b)) ||
+                (e = cudaEventElapsedTime(ms, a, b))))
+        st = cuda_fail(e, "timing");
+    if (ms && !st)
+        *ms /= (float)reps;
+    if (a)
+        cudaEventDestroy(a);
+    if (b)
+        cudaEventDestroy(b);
+    p->n_refl = keep;
+    const int st2 = plan_upload_desc(p, nullptr);
+    return st ? st : st2;
+}
+
+struct TuneKey {
+    int d0, d1, d2, nbucket;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(d0, d1, d2, nbucket) < std::tie(o.d0, o.d1, o.d2, o.nbucket);
+    }
+};
+struct TuneVal {
+    int variant, tile, morton;
+    float ms;
+};
+std::map<TuneKey, TuneVal> g_tune_cache;
+
+}  // namespace
+
+// A batch: several plans run by one persistent launch, optionally replayed
+// from a captured CUDA graph.
+struct anacor_batch {
+    std::vector<anacor_plan *> plans;
+    SampleDesc *d_descs = nullptr;
+    unsigned long long *d_counter = nullptr;
+    long long items = 0;
+    int variant = 0;
+    int grid = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+int batch_upload(anacor_batch *b)
+{
+    std::vector<SampleDesc> descs;
+    long long total = 0;
+    for (anacor_plan *p : b->plans) {
+        descs.push_back(plan_desc(p, total));
+        total += (long long)p->n_refl * p->tiles;
+    }
+    b->items = total;
+    b->grid = total ? grid_for(b->plans[0]->dev, b->variant, total) : 0;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice,
+                             b->stream)) ||
+        (e = cudaStreamSynchronize(b->stream)))
+        return cuda_fail(e, "descriptor upload");
+    // a captured graph holds the old grid: drop it
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return kOk;
+}
+
+int batch_check(anacor_batch *b, cudaStream_t st)
+{
+    cudaError_t e;
+    for (anacor_plan *p : b->plans) {
+        int status = 0;
+        if ((e = cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaStreamSynchronize(st)))
+            return cuda_fail(e, "status");
+        for (int bit = 1; bit < 16; bit++)
+            if (status & (1 << bit))
+                return fail(bit, status_text(bit));
+    }
+    return succeed();
 }
 
 }  // namespace
@@ -581,7 +738,7 @@ int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream)
         return cuda_fail(e, "descriptor upload");
     if (total > 0) {
         const int grid = plan_grid(p0, total);
-        if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st)))
+        if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st, p0->variant)))
             return cuda_fail(e, "kernel launch");
     }
     if ((e = cudaStreamSynchronize(st)))
@@ -832,6 +989,260 @@ int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *
         return st;
     }
     return succeed();
+}
+
+
+int anacor_plan_configure(anacor_plan *p, int variant, int tile, int morton)
+{
+    if (!p)
+        return fail(kErrArgs, "null plan");
+    if (int st = plan_configure(p, variant, tile, morton))
+        return st;
+    return succeed();
+}
+
+int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *morton)
+{
+    if (!p)
+        return fail(kErrArgs, "null plan");
+    if (variant)
+        *variant = p->variant ? p->variant : absorption_variant();
+    if (tile)
+        *tile = p->tile;
+    if (morton)
+        *morton = p->morton ? 1 : 0;
+    return succeed();
+}
+
+int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
+{
+    if (!p || p->n_refl <= 0 || p->n_vox <= 0)
+        return fail(kErrArgs, "autotune needs a plan with voxels and reflections");
+    int nb = 0;
+    while ((1 << nb) < p->n_vox)
+        nb++;
+    const TuneKey key{p->dims[0], p->dims[1], p->dims[2], nb};
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            const TuneVal v = it->second;
+            if (best_ms)
+                *best_ms = v.ms;
+            return plan_configure(p, v.variant, v.tile, v.morton) ? t_status : succeed();
+        }
+    }
+    static const int variants[] = {2, 3, 4};
+    static const int tiles[] = {1024, 2048, 4096};
+    TuneVal best{0, 0, 0, 1e30f};
+    for (int morton = 1; morton >= 0; morton--) {
+        for (int tile : tiles) {
+            for (int variant : variants) {
+                if (int st = plan_configure(p, variant, tile, morton))
+                    return st;
+                // enough reflections for a few waves of work items
+                const long long slots = (long long)p->dev->sms * variant_occupancy(p->dev, variant);
+                int64_t k = (int64_t)((4 * slots + p->tiles - 1) / p->tiles);
+                if (sample_refl > 0)
+                    k = std::max<int64_t>(k, sample_refl);
+                k = std::min<int64_t>(k, p->n_refl);
+                float ms = 0.0f;
+                if (int st = plan_time(p, k, 2, &ms))
+                    return st;
+                ms = ms * (float)p->n_refl / (float)k;
+                if (ms < best.ms)
+                    best = TuneVal{variant, tile, morton, ms};
+            }
+        }
+    }
+    if (int st = plan_configure(p, best.variant, best.tile, best.morton))
+        return st;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_tune_cache[key] = best;
+    }
+    if (best_ms)
+        *best_ms = best.ms;
+    return succeed();
+}
+
+anacor_batch *anacor_batch_create(anacor_plan *const *plans, int n_plans)
+{
+    if (!plans || n_plans <= 0) {
+        fail(kErrArgs, "empty batch");
+        return nullptr;
+    }
+    anacor_batch *b = new (std::nothrow) anacor_batch();
+    if (!b) {
+        fail(kErrNoMem, "out of host memory");
+        return nullptr;
+    }
+    for (int i = 0; i < n_plans; i++) {
+        if (!plans[i]) {
+            delete b;
+            fail(kErrArgs, "null plan in batch");
+            return nullptr;
+        }
+        b->plans.push_back(plans[i]);
+    }
+    b->stream = plans[0]->stream;
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->d_descs, sizeof(SampleDesc) * (size_t)n_plans)) ||
+        (e = cudaMalloc(&b->d_counter, sizeof(unsigned long long)))) {
+        cuda_fail(e, "device allocation");
+        anacor_batch_destroy(b);
+        return nullptr;
+    }
+    if (batch_upload(b)) {
+        const int keep = t_status;
+        const std::string msg = t_msg;
+        anacor_batch_destroy(b);
+        t_status = keep;
+        t_msg = msg;
+        return nullptr;
+    }
+    succeed();
+    return b;
+}
+
+int anacor_batch_configure(anacor_batch *b, int variant)
+{
+    if (!b || variant < 0 || variant > 4)
+        return fail(kErrArgs, "bad arguments");
+    b->variant = variant;
+    if (int st = batch_upload(b))
+        return st;
+    return succeed();
+}
+
+int anacor_batch_launch(anacor_batch *b, void *stream)
+{
+    if (!b)
+        return fail(kErrArgs, "null batch");
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+    if (b->items > 0) {
+        cudaError_t e = launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st,
+                                          b->variant);
+        if (e)
+            return cuda_fail(e, "kernel launch");
+    }
+    return succeed();
+}
+
+int anacor_batch_capture(anacor_batch *b, void *stream)
+{
+    if (!b)
+        return fail(kErrArgs, "null batch");
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    cudaError_t e;
+    if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)))
+        return cuda_fail(e, "cudaStreamBeginCapture");
+    cudaError_t le = cudaSuccess;
+    if (b->items > 0)
+        le = launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st, b->variant);
+    e = cudaStreamEndCapture(st, &b->graph);
+    if (le)
+        return cuda_fail(le, "kernel launch during capture");
+    if (e)
+        return cuda_fail(e, "cudaStreamEndCapture");
+    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)))
+        return cuda_fail(e, "cudaGraphInstantiate");
+    return succeed();
+}
+
+int anacor_batch_replay(anacor_batch *b, void *stream)
+{
+    if (!b || !b->exec)
+        return fail(kErrArgs, "batch has no captured graph");
+    cudaError_t e = cudaGraphLaunch(b->exec, stream ? (cudaStream_t)stream : b->stream);
+    if (e)
+        return cuda_fail(e, "cudaGraphLaunch");
+    return succeed();
+}
+
+int anacor_batch_wait(anacor_batch *b, void *stream)
+{
+    if (!b)
+        return fail(kErrArgs, "null batch");
+    return batch_check(b, stream ? (cudaStream_t)stream : b->stream);
+}
+
+int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl)
+{
+    if (!b)
+        return fail(kErrArgs, "null batch");
+    // per-sample tile and voxel order, then one register-budget variant for the launch
+    for (anacor_plan *p : b->plans)
+        if (p->n_refl > 0 && p->n_vox > 0)
+            if (int st = anacor_plan_autotune(p, sample_refl, nullptr))
+                return st;
+    float best = 1e30f;
+    int best_v = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int v : {2, 3, 4}) {
+        b->variant = v;
+        if (int st = batch_upload(b))
+            return st;
+        anacor_batch_launch(b, nullptr);   // warm-up
+        cudaEventRecord(e0, b->stream);
+        anacor_batch_launch(b, nullptr);
+        cudaEventRecord(e1, b->stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e || (e = cudaEventElapsedTime(&ms, e0, e1))) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(e, "timing");
+        }
+        if (ms < best) {
+            best = ms;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->variant = best_v;
+    if (int st = batch_upload(b))
+        return st;
+    return succeed();
+}
+
+int anacor_batch_info(const anacor_batch *b, int *grid, long long *items, int *variant)
+{
+    if (!b)
+        return fail(kErrArgs, "null batch");
+    if (grid)
+        *grid = b->grid;
+    if (items)
+        *items = b->items;
+    if (variant)
+        *variant = b->variant ? b->variant : absorption_variant();
+    return succeed();
+}
+
+void anacor_batch_destroy(anacor_batch *b)
+{
+    if (!b)
+        return;
+    if (b->exec)
+        cudaGraphExecDestroy(b->exec);
+    if (b->graph)
+        cudaGraphDestroy(b->graph);
+    if (b->d_descs)
+        cudaFree(b->d_descs);
+    if (b->d_counter)
+        cudaFree(b->d_counter);
+    delete b;
 }
 
 }  // extern "C"

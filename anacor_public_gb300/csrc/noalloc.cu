@@ -181,6 +181,7 @@ extern "C" int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *s
     desc.refl = d_tables;
     desc.n_refl = n_refl;
     desc.tiles = (int)tiles;
+    desc.tile = kTile;
     desc.full_iteration = full_iteration;
     desc.is_exp = is_exp;
     desc.out = d_out;

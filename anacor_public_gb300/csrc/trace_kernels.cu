@@ -614,8 +614,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         float s = 0.0f, c = 0.0f;
         int bad = kOk;
         unsigned nsteps = 0;
-        const int v0 = t * kTile;
-        const int v1 = min(D.n_vox, v0 + kTile);
+        const int v0 = t * D.tile;
+        const int v1 = min(D.n_vox, v0 + D.tile);
         // every lane runs the same number of iterations (the march is warp-synchronous)
         for (int vb = v0; vb < v1; vb += kBlock) {
             const int vi = vb + tid;
@@ -835,14 +835,14 @@ int absorption_variant()
 }
 
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,
-                              unsigned long long *d_counter, int grid, cudaStream_t st)
+                              unsigned long long *d_counter, int grid, cudaStream_t st, int variant)
 {
     if (total_items <= 0)
         return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess)
         return e;
-    switch (absorption_variant()) {
+    switch (variant > 0 ? variant : absorption_variant()) {
     case 1: absorption_kernel<1><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
     case 3: absorption_kernel<3><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
     case 4: absorption_kernel<4><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
@@ -866,10 +866,10 @@ cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const
 
 int absorption_block_threads() { return kBlock; }
 
-int absorption_occupancy(int *blocks_per_sm)
+int absorption_occupancy(int *blocks_per_sm, int variant)
 {
     cudaError_t e;
-    switch (absorption_variant()) {
+    switch (variant > 0 ? variant : absorption_variant()) {
     case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<1>, kBlock, 0); break;
     case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<3>, kBlock, 0); break;
     case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<4>, kBlock, 0); break;

@@ -7,9 +7,10 @@
 
 namespace anacor {
 
-// Voxels per work item (one CTA pass).  A sample with N voxels and R
-// reflections is R * ceil(N / kTile) work items.
+// Voxels per work item (one CTA pass) unless a sample sets its own: a sample
+// with N voxels and R reflections is R * ceil(N / tile) work items.
 constexpr int kTile = 2048;
+constexpr int kMinTile = 512;
 
 // One sample (volume + voxel list + reflections) of a launch.  All pointers
 // are device pointers.
@@ -20,10 +21,10 @@ struct SampleDesc {
     const short4 *coords;   // (z, y, x, 0)
     const ReflTable *refl;  // [n_refl]
     long long n_refl;
-    int tiles;              // ceil(n_vox / kTile)
+    int tiles;              // ceil(n_vox / tile)
+    int tile;               // voxels per work item
     int full_iteration;
     int is_exp;
-    int pad;
     double mu[4];           // [liquor, loop, crystal, bubble]
     double voxel[3];        // z, y, x
     double *out;            // [n_refl]
@@ -39,8 +40,9 @@ struct SampleDesc {
 
 int rcp_table_init();
 int absorption_block_threads();
-int absorption_occupancy(int *blocks_per_sm);
-// register-budget variant of the absorption kernel in use (CTAs per SM it targets)
+// CTAs per SM of a register-budget variant (1..4; 0 = the process default)
+int absorption_occupancy(int *blocks_per_sm, int variant = 0);
+// the process-default register-budget variant (CTAs per SM it targets)
 int absorption_variant();
 
 cudaError_t launch_pack_coords(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
@@ -51,7 +53,7 @@ cudaError_t launch_pack_coords_morton(const long long *d_c, int n, const int *di
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs
 // take items from `d_counter` (reset inside the launch sequence).
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,
-                              unsigned long long *d_counter, int grid, cudaStream_t st);
+                              unsigned long long *d_counter, int grid, cudaStream_t st, int variant = 0);
 cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const int *dims, const short4 *d_coords,
                               int n, const double *d_voxel, int full, const double *d_sq, int sq_stride,
                               const double *d_qtab, int *face, int *len, int *nseg, int *first, int *last, double *L,

@@ -196,17 +196,22 @@ def high_absorption_sample(n_refl: int = 50000, stride: int = 1, seed: int = 4) 
 
 
 def batch_samples(n_samples: int = 12, seed: int = 2, refl_range=(2000, 60000),
-                  dim_range=(128, 640), max_refl: int | None = None):
-    """Independent samples with log-uniform dimensions, 15-40% semi-axes and mu jitter +-30%.
+                  dim_range=(128, 640), max_refl: int | None = None, voxel_budget: int = 60000,
+                  strides=(2, 4, 8)):
+    """Independent samples with log-uniform dimensions, crystal diameters 15-40%
+    of the smallest dimension, the same label recipe, mu jittered +-30% and
+    log-uniform reflection counts.
 
-    Axes are sorted so the largest is last (the reference's path buffer holds
-    x_max*sqrt(3) entries, ``AnACor/src/ray_tracing_basic.c:402-406``).
+    The crystal-voxel sampling stride of each sample is the smallest of
+    `strides` that keeps its voxel list within `voxel_budget` (the largest
+    stride otherwise).  Axes are sorted so the largest is last (the reference's
+    path buffer holds x_max*sqrt(3) entries, ``AnACor/src/ray_tracing_basic.c:402-406``).
     """
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n_samples):
         dims = np.exp(rng.uniform(math.log(dim_range[0]), math.log(dim_range[1]), size=3)).astype(int)
-        dims = np.sort(dims)[::-1].copy()  # z >= y >= x ... then put the largest last
+        dims = np.sort(dims)[::-1].copy()
         dims = np.array([dims[1], dims[2], dims[0]])
         frac = rng.uniform(0.15, 0.40, size=3)
         semi = frac * float(np.min(dims)) / 2.0
@@ -215,10 +220,19 @@ def batch_samples(n_samples: int = 12, seed: int = 2, refl_range=(2000, 60000),
             n_refl = min(n_refl, max_refl)
         mu = MU_BASE * rng.uniform(0.7, 1.3, size=4)
         scale = float(np.min(dims)) / 96.0
+        sample_seed = int(rng.integers(1 << 30))
         # the loop grazes the liquor so that rays can cross liquor -> loop
-        s = make_sample(shape=tuple(int(d) for d in dims), n_refl=n_refl, seed=int(rng.integers(1 << 30)),
-                        mu=mu, semi_axes=tuple(semi), shell=6.0 * scale,
+        s = make_sample(shape=tuple(int(d) for d in dims), n_refl=n_refl, seed=sample_seed, mu=mu,
+                        semi_axes=tuple(semi), shell=6.0 * scale,
                         torus=(float(np.max(semi)) + 7.0 * scale, 3.0 * scale),
                         bubble_r=3.0 * scale, name=f"batch{k}")
+        n_all = int(np.count_nonzero(s.label == CRYSTAL))
+        stride = strides[-1]
+        for st in strides:
+            if n_all / st ** 3 <= voxel_budget:
+                stride = st
+                break
+        s.coords = crystal_coords(s.label, stride)
+        s.name = f"batch{k}_stride{stride}"
         out.append(s)
     return out

@@ -88,6 +88,23 @@ class Plan:
         _lib.check(self._L.anacor_plan_count_steps(self._h, ct.byref(n)), self._L)
         return int(n.value)
 
+    def configure(self, variant: int = 0, tile: int = 0, morton: int = -1):
+        """Execution parameters: kernel register-budget variant (CTAs/SM), voxels
+        per work item, Morton voxel order (1) or the caller's order (0)."""
+        _lib.check(self._L.anacor_plan_configure(self._h, int(variant), int(tile), int(morton)), self._L)
+
+    def config(self) -> dict:
+        v, t, m = ct.c_int(), ct.c_int(), ct.c_int()
+        _lib.check(self._L.anacor_plan_config(self._h, ct.byref(v), ct.byref(t), ct.byref(m)), self._L)
+        return {"variant": v.value, "tile": t.value, "morton": m.value}
+
+    def autotune(self, sample_refl: int = 0) -> float:
+        """Pick the fastest (variant, tile, order) on a reflection sample; returns
+        the estimated ms for all reflections."""
+        ms = ct.c_float()
+        _lib.check(self._L.anacor_plan_autotune(self._h, int(sample_refl), ct.byref(ms)), self._L)
+        return float(ms.value)
+
     def launch_info(self):
         g, k = ct.c_int(), ct.c_int()
         _lib.check(self._L.anacor_plan_launch_info(self._h, ct.byref(g), ct.byref(k)), self._L)
@@ -96,6 +113,58 @@ class Plan:
     def close(self):
         if getattr(self, "_h", None):
             self._L.anacor_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several plans in one persistent launch; optionally captured in a CUDA graph."""
+
+    def __init__(self, plans):
+        self._L = _lib.load()
+        self.plans = list(plans)
+        arr = (ct.c_void_p * len(self.plans))(*[p._h.value for p in self.plans])
+        h = self._L.anacor_batch_create(arr, len(self.plans))
+        if not h:
+            st, msg = _lib.last_error(self._L)
+            raise _lib.AnacorError(st, msg)
+        self._h = ct.c_void_p(h)
+
+    def configure(self, variant: int = 0):
+        _lib.check(self._L.anacor_batch_configure(self._h, int(variant)), self._L)
+
+    def autotune(self, sample_refl: int = 0):
+        _lib.check(self._L.anacor_batch_autotune(self._h, int(sample_refl)), self._L)
+
+    def launch(self, stream: int | None = None):
+        _lib.check(self._L.anacor_batch_launch(self._h, ct.c_void_p(stream or 0)), self._L)
+
+    def capture(self, stream: int):
+        """Capture one launch into a CUDA graph (needs a non-default stream)."""
+        _lib.check(self._L.anacor_batch_capture(self._h, ct.c_void_p(stream)), self._L)
+
+    def replay(self, stream: int | None = None):
+        _lib.check(self._L.anacor_batch_replay(self._h, ct.c_void_p(stream or 0)), self._L)
+
+    def wait(self, stream: int | None = None):
+        _lib.check(self._L.anacor_batch_wait(self._h, ct.c_void_p(stream or 0)), self._L)
+
+    def info(self) -> dict:
+        g, n, v = ct.c_int(), ct.c_longlong(), ct.c_int()
+        _lib.check(self._L.anacor_batch_info(self._h, ct.byref(g), ct.byref(n), ct.byref(v)), self._L)
+        return {"grid": g.value, "items": n.value, "variant": v.value}
+
+    def results(self, stream: int | None = None):
+        return [p.result(stream) for p in self.plans]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.anacor_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -128,9 +128,39 @@ int anacor_plan_count_steps(anacor_plan *p, uint64_t *total);
 int anacor_plan_launch_info(const anacor_plan *p, int *grid, int *kernels);
 void anacor_plan_destroy(anacor_plan *p);
 
+/* Execution parameters of a plan (no counterpart in the reference; they do
+ * not change the per-ray results, only the FP32 summation order of A_h):
+ * variant = register-budget variant of the kernel, i.e. the CTAs per SM it is
+ * compiled for (1..4, 0 = process default); tile = voxels per work item
+ * (>= 512, 0 = unchanged); morton = 1 to pack the voxel list in Morton order,
+ * 0 for the caller's order, -1 unchanged. */
+int anacor_plan_configure(anacor_plan *p, int variant, int tile, int morton);
+int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *morton);
+/* Autotuner: times every (variant, tile, order) candidate on the first
+ * reflections of the plan (at least sample_refl of them) and keeps the
+ * fastest; results are cached per volume shape and voxel-count class.
+ * *best_ms = the chosen configuration's time scaled to all reflections. */
+int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms);
+
 /* One persistent launch over several plans (independent samples with their
  * own volumes, voxel lists and reflections).  Results land in each plan. */
 int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream);
+
+/* A batch object: the same launch kept ready for repeated runs, optionally
+ * captured once into a CUDA graph and replayed.  The plans must outlive it;
+ * after a plan's reflections or configuration change, call
+ * anacor_batch_configure to refresh it. */
+typedef struct anacor_batch anacor_batch;
+anacor_batch *anacor_batch_create(anacor_plan *const *plans, int n_plans);
+int anacor_batch_configure(anacor_batch *b, int variant);
+int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl);
+int anacor_batch_launch(anacor_batch *b, void *stream);
+int anacor_batch_capture(anacor_batch *b, void *stream);
+int anacor_batch_replay(anacor_batch *b, void *stream);
+/* synchronise `stream` and check every plan's device status word */
+int anacor_batch_wait(anacor_batch *b, void *stream);
+int anacor_batch_info(const anacor_batch *b, int *grid, long long *items, int *variant);
+void anacor_batch_destroy(anacor_batch *b);
 
 /* ------------------------------------------------- no-allocation entry -- */
 

@@ -1,0 +1,84 @@
+"""Execution parameters, the autotuner, batches and CUDA-graph replay: any
+configuration gives A_h within 1e-6 of the oracle, and a fixed configuration
+is bit-reproducible."""
+import os
+
+import numpy as np
+import pytest
+
+from anacor_public_gb300 import build, synth, tracer
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-6
+
+
+def max_rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.abs(np.asarray(b))))
+
+
+@pytest.fixture(scope="module")
+def sample():
+    build.build()
+    return synth.small_sample(n_refl=48, seed=9)
+
+
+@pytest.fixture(scope="module")
+def want(sample, oracle):
+    return oracle.overall(sample, threads=os.cpu_count() or 1)
+
+
+@pytest.mark.parametrize("variant", [2, 3, 4])
+@pytest.mark.parametrize("tile", [512, 2048, 8192])
+@pytest.mark.parametrize("morton", [0, 1])
+def test_every_configuration_matches_the_oracle(sample, want, variant, tile, morton):
+    p = tracer.Plan.from_sample(sample)
+    p.configure(variant, tile, morton)
+    assert p.config() == {"variant": variant, "tile": tile, "morton": morton}
+    p.run()
+    a = p.result()
+    p.run()
+    assert np.array_equal(a, p.result())
+    assert max_rel(a, want) <= RTOL
+    p.close()
+
+
+def test_autotune_keeps_results(sample, want):
+    p = tracer.Plan.from_sample(sample)
+    ms = p.autotune()
+    assert ms > 0
+    cfg = p.config()
+    assert cfg["variant"] in (2, 3, 4) and cfg["tile"] in (1024, 2048, 4096)
+    p.run()
+    assert max_rel(p.result(), want) <= RTOL
+    # a second plan of the same shape class takes the cached choice
+    q = tracer.Plan.from_sample(sample)
+    q.autotune()
+    assert q.config() == cfg
+    p.close()
+    q.close()
+
+
+def test_batch_launch_and_graph_replay(oracle):
+    import torch
+    samples = synth.batch_samples(n_samples=3, max_refl=24, dim_range=(64, 128))
+    plans = [tracer.Plan.from_sample(s) for s in samples]
+    wants = [oracle.overall(s, threads=os.cpu_count() or 1) for s in samples]
+    b = tracer.Batch(plans)
+    b.autotune()
+    st = torch.cuda.Stream()
+    b.launch(st.cuda_stream)
+    b.wait(st.cuda_stream)
+    first = b.results(st.cuda_stream)
+    for got, w in zip(first, wants):
+        assert max_rel(got, w) <= RTOL
+    b.capture(st.cuda_stream)
+    for _ in range(2):
+        b.replay(st.cuda_stream)
+    b.wait(st.cuda_stream)
+    for got, f in zip(b.results(st.cuda_stream), first):
+        assert np.array_equal(got, f)
+    info = b.info()
+    assert info["items"] > 0 and info["grid"] > 0
+    b.close()
+    for p in plans:
+        p.close()

@@ -295,13 +295,15 @@ __device__ __noinline__ void march_lane(const FaceRule &R, const LegGeom &g, int
 
 // Label of increment `inc` from the reference's FP64 expression (an
 // increment whose fixed-point fraction lies near a rounding boundary).
-__device__ __noinline__ uint32_t exact_label(const FaceRule &G, const LegGeom &g, int ga, int gb, int inc, int ds,
-                                             int Ss, int Sa, int Sb, const int8_t *vol)
+__device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol &v)
 {
-    const int pa = exact_axis(g.ca, inc, G.q[ga], G.use_round, g.ha + 1);
-    const int pb = exact_axis(g.cb, inc, G.q[gb], G.use_round, g.hb + 1);
-    const int ps = g.cs + inc * ds;
-    return (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(vol) + ps * Ss + pa * Sa + pb * Sb);
+    int pz, py, px;
+    const int s = G.count_axis;
+    const int ds = G.q[s] > 0.0 ? 1 : -1;
+    pz = s == 0 ? cz + inc * ds : exact_axis(cz, inc, G.q[0], G.use_round, v.dz);
+    py = s == 1 ? cy + inc * ds : exact_axis(cy, inc, G.q[1], G.use_round, v.dy);
+    px = s == 2 ? cx + inc * ds : exact_axis(cx, inc, G.q[2], G.use_round, v.dx);
+    return (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(v.p) + (pz * v.dy + py) * v.dx + px);
 }
 
 struct LegResult {
@@ -352,46 +354,48 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         out.status = kErrNoFace;
         need = false;
     }
-    const FaceRule &R = rules[face > 0 ? face - 1 : 0];
-    if (need && R.status) {
-        out.status = R.status;
+    if (need && rules[face - 1].status) {
+        out.status = rules[face - 1].status;
         need = false;
-    }
-    int steps = 0;
-    LegGeom g;
-    leg_geom(R, cz, cy, cx, v, g);
-    if (need) {
-        const int cc = pick3(R.count_axis, cz, cy, cx);
-        const int dd = pick3(R.count_axis, v.dz, v.dy, v.dx);
-        steps = R.count_kind == 0 ? cc + 1 : (R.count_kind == 1 ? dd - cc : dd - cc + 1);
     }
     March m;
     m.last_i = 0; m.nseg = 1; m.vac = 0; m.prev = 0;
     Sink sk;
     sk.seg = seg;
 
-    // ---- cooperative eligibility and increment 0
-    bool coop = need && R.fast && !full && steps >= 1;
-    // the last increment of a count_kind 2 face clamps the step axis; it is
-    // taken separately after the cooperative part
-    const int steps_eff = R.count_kind == 2 ? steps - 1 : steps;
-    if (coop && steps_eff > 1) {
-        const long long ena = g.off + (long long)(steps_eff - 1) * g.Qa;
-        const long long enb = g.off + (long long)(steps_eff - 1) * g.Qb;
-        const int a1 = g.ca + (int)((g.off + g.Qa) >> 32), an = g.ca + (int)(ena >> 32);
-        const int b1 = g.cb + (int)((g.off + g.Qb) >> 32), bn = g.cb + (int)(enb >> 32);
-        coop = min(a1, an) >= 1 && max(a1, an) <= g.ha - 1 && min(b1, bn) >= 1 && max(b1, bn) <= g.hb - 1;
-    }
-    const int base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
-    bool stopped = false, live = false;
-    if (coop) {
-        seg[0] = (uint16_t)(3 << 13);
-        const int lab0 = __ldg(v.p + base);
-        if (lab0 == 0) {
-            stopped = true;
-        } else {
-            m.prev = lab0;
-            live = steps_eff > 1;
+    // ---- set-up: step count, cooperative eligibility, increment 0.  Only a
+    // few values cross the cooperative loop; the geometry is recomputed after.
+    bool coop = false, stopped = false, live = false;
+    int lim = 0, base = 0;
+    if (need) {
+        const FaceRule &R = rules[face - 1];
+        LegGeom g;
+        leg_geom(R, cz, cy, cx, v, g);
+        const int cc = pick3(R.count_axis, cz, cy, cx);
+        const int dd = pick3(R.count_axis, v.dz, v.dy, v.dx);
+        const int steps = R.count_kind == 0 ? cc + 1 : (R.count_kind == 1 ? dd - cc : dd - cc + 1);
+        // the last increment of a count_kind 2 face clamps the step axis; it is
+        // taken separately after the cooperative part
+        const int steps_eff = R.count_kind == 2 ? steps - 1 : steps;
+        coop = R.fast && !full && steps >= 1;
+        if (coop && steps_eff > 1) {
+            const long long ena = g.off + (long long)(steps_eff - 1) * g.Qa;
+            const long long enb = g.off + (long long)(steps_eff - 1) * g.Qb;
+            const int a1 = g.ca + (int)((g.off + g.Qa) >> 32), an = g.ca + (int)(ena >> 32);
+            const int b1 = g.cb + (int)((g.off + g.Qb) >> 32), bn = g.cb + (int)(enb >> 32);
+            coop = min(a1, an) >= 1 && max(a1, an) <= g.ha - 1 && min(b1, bn) >= 1 && max(b1, bn) <= g.hb - 1;
+        }
+        if (coop) {
+            base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
+            seg[0] = (uint16_t)(3 << 13);
+            const int lab0 = __ldg(v.p + base);
+            if (lab0 == 0) {
+                stopped = true;
+            } else {
+                m.prev = lab0;
+                live = steps_eff > 1;
+                lim = steps_eff;
+            }
         }
     }
 
@@ -403,62 +407,73 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         pend &= ~grp;
         const bool mine = (grp >> lane) & 1u;
         const FaceRule &G = rules[f - 1];
-        const int gs = G.count_axis, ga = gs == 0 ? 1 : 0, gb = gs == 2 ? 1 : 2;
-        const int sz = v.dy * v.dx, sy = v.dx;
-        const int Ss = pick3(gs, sz, sy, 1), Sa = pick3(ga, sz, sy, 1), Sb = pick3(gb, sz, sy, 1);
-        const int ds = G.q[gs] > 0.0 ? 1 : -1;
-        const long long Qa = G.Q[ga], Qb = G.Q[gb];
-        const uint32_t Ma = ((G.exact_mask >> ga) & 1) ? 0u : kAmbiguityMargin;
-        const uint32_t Mb = ((G.exact_mask >> gb) & 1) ? 0u : kAmbiguityMargin;
-        const long long off = G.use_round ? 0x80000000ll : 0ll;
-        const int lim = mine ? steps_eff : 0;
-        const int gmax = __reduce_max_sync(kAll, lim);
+        const int glim = mine ? lim : 0;
+        const int gmax = __reduce_max_sync(kAll, glim);
         const uint8_t *p = reinterpret_cast<const uint8_t *>(v.p) + base;
         bool on = mine && live;
         uint32_t prev4 = (uint32_t)(uint8_t)m.prev * 0x01010101u;
         for (int i0 = 1; i0 < gmax; i0 += 32) {
             if (!__any_sync(kAll, on))
                 break;
-            const int i = i0 + lane;
-            const long long ea = off + (long long)i * Qa, eb = off + (long long)i * Qb;
-            const bool amb = ((uint32_t)ea + Ma < 2u * Ma) | ((uint32_t)eb + Mb < 2u * Mb);
-            const int delta = i * ds * Ss + (int)(ea >> 32) * Sa + (int)(eb >> 32) * Sb;
-            const unsigned ambm = __ballot_sync(kAll, amb);
+            int delta;
+            unsigned ambm;
+            {
+                // group constants, re-read from shared memory per chunk
+                const int gs = G.count_axis, ga = gs == 0 ? 1 : 0, gb = gs == 2 ? 1 : 2;
+                const int sz = v.dy * v.dx, sy = v.dx;
+                const int ds = G.q[gs] > 0.0 ? 1 : -1;
+                const long long off = G.use_round ? 0x80000000ll : 0ll;
+                const uint32_t Ma = ((G.exact_mask >> ga) & 1) ? 0u : kAmbiguityMargin;
+                const uint32_t Mb = ((G.exact_mask >> gb) & 1) ? 0u : kAmbiguityMargin;
+                const int i = i0 + lane;
+                const long long ea = off + (long long)i * G.Q[ga], eb = off + (long long)i * G.Q[gb];
+                const bool amb = ((uint32_t)ea + Ma < 2u * Ma) | ((uint32_t)eb + Mb < 2u * Mb);
+                delta = i * ds * pick3(gs, sz, sy, 1) + (int)(ea >> 32) * pick3(ga, sz, sy, 1) +
+                        (int)(eb >> 32) * pick3(gb, sz, sy, 1);
+                ambm = __ballot_sync(kAll, amb);
+            }
 #pragma unroll 1
             for (int t = 0; t < 32; t += kMarchBatch) {
                 if (!__any_sync(kAll, on))
                     break;
                 const int ib = i0 + t;
+                const int n = on ? glim - ib : 0;   // increments this lane still takes
+                // kMarchBatch label loads in flight per lane before any is checked
                 uint32_t lb[kMarchBatch];
 #pragma unroll
                 for (int k = 0; k < kMarchBatch; k++) {
                     const int dk = __shfl_sync(kAll, delta, t + k);
-                    lb[k] = (on && ib + k < lim) ? (uint32_t)__ldg(p + dk) : 0u;
+                    lb[k] = k < n ? (uint32_t)__ldg(p + dk) : 0u;
                 }
                 const unsigned amb_here = (ambm >> t) & ((1u << kMarchBatch) - 1u);
                 if (amb_here) {
                     // the reference's FP64 expression decides, per lane (c enters its rounding)
                     for (int k = 0; k < kMarchBatch; k++)
-                        if (((amb_here >> k) & 1u) && on && ib + k < lim)
-                            lb[k] = exact_label(G, g, ga, gb, ib + k, ds, Ss, Sa, Sb, v.p);
+                        if (((amb_here >> k) & 1u) && k < n)
+                            lb[k] = exact_label(G, cz, cy, cx, ib + k, v);
                 }
-                if (on) {
-                    // Four increments per packed word; the bytes that are zero
-                    // (stop) or differ from the previous label (class change)
-                    // are found with SIMD byte compares and handled one event
-                    // at a time, in increment order.
-                    const int n = lim - ib;
+                if (n > 0) {
+                    // Four increments per packed word.  prev is never 0 here, so
+                    // a word equal to prev4 holds neither a stop nor a class
+                    // change: the common case costs one compare per word.
+                    const uint32_t w0 = lb[0] | (lb[1] << 8) | (lb[2] << 16) | (lb[3] << 24);
+                    const uint32_t w1 = lb[4] | (lb[5] << 8) | (lb[6] << 16) | (lb[7] << 24);
+                    if (n >= kMarchBatch && w0 == prev4 && w1 == prev4) {
+                        m.last_i = ib + kMarchBatch - 1;
+                    } else {
 #pragma unroll
-                    for (int q = 0; q < kMarchBatch / 4; q++) {
-                        const int b4 = ib + 4 * q;
-                        const int nq = n - 4 * q;
-                        if (!stopped && nq > 0) {
-                            const uint32_t w = lb[4 * q] | (lb[4 * q + 1] << 8) | (lb[4 * q + 2] << 16) |
-                                               (lb[4 * q + 3] << 24);
+                        for (int q = 0; q < 2; q++) {
+                            const int nq = n - 4 * q;
+                            if (stopped || nq <= 0)
+                                break;
+                            const uint32_t w = q == 0 ? w0 : w1;
+                            const int b4 = ib + 4 * q;
                             const uint32_t valid_bytes = nq >= 4 ? 0xffffffffu : (1u << (8 * nq)) - 1u;
-                            uint32_t ev = (__vcmpne4(w, prev4) | __vcmpeq4(w, 0u)) & valid_bytes;
-                            while (ev) {
-                                const int byte = (__ffs(ev) - 1) >> 3;
+                            // the lowest set bit of w ^ prev4 lies in the first byte
+                            // that differs: a stop (0) or a class change
+                            uint32_t x = (w ^ prev4) & valid_bytes;
+                            while (x) {
+                                const int byte = (__ffs(x) - 1) >> 3;
                                 const int lab = (int)(signed char)(w >> (8 * byte));
                                 const int inc = b4 + byte;
                                 if (lab == 0) {
@@ -473,20 +488,30 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
                                 }
                                 m.prev = lab;
                                 prev4 = (uint32_t)(uint8_t)lab * 0x01010101u;
-                                ev = (__vcmpne4(w, prev4) | __vcmpeq4(w, 0u)) & valid_bytes &
-                                     (byte == 3 ? 0u : (0xffffffffu << (8 * (byte + 1))));
+                                const uint32_t above = byte == 3 ? 0u : (0xffffffffu << (8 * (byte + 1)));
+                                x = (w ^ prev4) & valid_bytes & above;
                             }
                             if (!stopped)
                                 m.last_i = b4 + min(nq, 4) - 1;
                         }
                     }
-                    if (stopped || ib + kMarchBatch >= lim)
+                    if (stopped || n <= kMarchBatch)
                         on = false;
                 }
             }
         }
     }
-    if (coop && !stopped && steps_eff < steps) {
+    if (!need)
+        return;
+
+    // ---- after the march: geometry again, the per-lane paths, lengths
+    const FaceRule &R = rules[face - 1];
+    LegGeom g;
+    leg_geom(R, cz, cy, cx, v, g);
+    const int cc = pick3(R.count_axis, cz, cy, cx);
+    const int dd = pick3(R.count_axis, v.dz, v.dy, v.dx);
+    const int steps = R.count_kind == 0 ? cc + 1 : (R.count_kind == 1 ? dd - cc : dd - cc + 1);
+    if (coop && !stopped && R.count_kind == 2) {
         // the clamped last increment of a count_kind 2 face
         int pz, py, px;
         const int inc = steps - 1;
@@ -495,10 +520,8 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         if (inc >= 1)
             visit<0>(m, sk, inc, lab, 0, R.vac_limit);
     }
-    if (need && !coop)
+    if (!coop)
         march_lane<0>(R, g, cz, cy, cx, steps, v, full, m, sk);
-    if (!need)
-        return;
 
     // ---- cal_path2_plus
     const int len = m.last_i + 1;
@@ -585,6 +608,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
 {
     __shared__ ReflTable tab;
     __shared__ uint16_t seg[kMaxSegments * kBlock];
+    __shared__ double lsum[4][kBlock];
     __shared__ float red_s[kWarps], red_c[kWarps];
     __shared__ long long item_s;
     __shared__ int last_s;
@@ -621,7 +645,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             const int vi = vb + tid;
             const bool valid = vi < v1;
             const short4 cv = valid ? __ldg(D.coords + vi) : make_short4(0, 0, 0, 0);
-            double Ls[4];
 #pragma unroll 1
             for (int leg = 0; leg < 2; leg++) {
                 LegResult a;
@@ -629,21 +652,19 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
                                  D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
                 bad |= a.status;
                 nsteps += valid ? (unsigned)a.len : 0u;
-                if (leg == 0) {
-                    for (int k = 0; k < 4; k++)
-                        Ls[k] = a.L[k];
-                } else {
-                    // (L_incident + L_diffracted) per class, as cal_rate adds them
-                    for (int k = 0; k < 4; k++)
-                        Ls[k] = __dadd_rn(Ls[k], a.L[k]);
-                }
+                // the incident leg's lengths wait in shared memory while the
+                // diffracted leg marches; then (L_incident + L_diffracted) per
+                // class, as cal_rate adds them
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    lsum[k][tid] = leg == 0 ? a.L[k] : __dadd_rn(lsum[k][tid], a.L[k]);
             }
             if (valid) {
                 // cal_rate's exponent, operand order of AnACor/src/ray_tracing_basic.c:1573-1576
-                const double t0 = __dmul_rn(D.mu[0], Ls[0]);
-                const double t1 = __dmul_rn(D.mu[1], Ls[1]);
-                const double t2 = __dmul_rn(D.mu[2], Ls[2]);
-                const double t3 = __dmul_rn(D.mu[3], Ls[3]);
+                const double t0 = __dmul_rn(D.mu[0], lsum[0][tid]);
+                const double t1 = __dmul_rn(D.mu[1], lsum[1][tid]);
+                const double t2 = __dmul_rn(D.mu[2], lsum[2][tid]);
+                const double t3 = __dmul_rn(D.mu[3], lsum[3][tid]);
                 const double ex = __dadd_rn(__dadd_rn(__dadd_rn(t0, t1), t2), t3);
                 const float term = D.is_exp ? exp_neg(ex) : (float)ex;
                 float ns, e;

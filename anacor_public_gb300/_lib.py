@@ -17,6 +17,7 @@ _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _i8p = np.ctypeslib.ndpointer(dtype=np.int8, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _i8ppp = ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8)))
 
 # every symbol declared in include/anacor_gb300.h
@@ -30,6 +31,12 @@ EXPORTS = (
     "anacor_plan_configure", "anacor_plan_config", "anacor_plan_autotune", "anacor_batch_create",
     "anacor_batch_configure", "anacor_batch_autotune", "anacor_batch_launch", "anacor_batch_capture",
     "anacor_batch_replay", "anacor_batch_wait", "anacor_batch_info", "anacor_batch_destroy",
+    "anacor_surrogate_create", "anacor_surrogate_destroy", "anacor_surrogate_param_count",
+    "anacor_surrogate_members", "anacor_surrogate_params", "anacor_surrogate_fourier", "anacor_surrogate_scale",
+    "anacor_surrogate_inputs", "anacor_surrogate_inputs_device", "anacor_surrogate_set_data",
+    "anacor_surrogate_train", "anacor_surrogate_gradients", "anacor_surrogate_predict",
+    "anacor_surrogate_predict_device", "anacor_surrogate_audit_flags", "anacor_surrogate_save",
+    "anacor_surrogate_load", "anacor_tc_gemm_check",
 )
 
 _LIB = None
@@ -142,6 +149,31 @@ def load(path: str | None = None) -> ct.CDLL:
                                     ct.POINTER(ct.c_int)]
     L.anacor_batch_destroy.restype = None
     L.anacor_batch_destroy.argtypes = [ct.c_void_p]
+    # learned surrogate
+    _vp, _int = ct.c_void_p, ct.c_int
+    sigs = {
+        "anacor_surrogate_create": (_vp, [_int, ct.c_uint32, ct.c_float]),
+        "anacor_surrogate_destroy": (None, [_vp]),
+        "anacor_surrogate_param_count": (ct.c_int64, []),
+        "anacor_surrogate_members": (_int, [_vp]),
+        "anacor_surrogate_params": (_int, [_vp, _f32p, _int]),
+        "anacor_surrogate_fourier": (_int, [_vp, _f32p, _int]),
+        "anacor_surrogate_scale": (_int, [_vp, ct.POINTER(ct.c_double), ct.POINTER(ct.c_double), _int]),
+        "anacor_surrogate_inputs": (_int, [_f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p, _f32p]),
+        "anacor_surrogate_inputs_device": (_int, [_vp, _vp, ct.c_int64, _f64p, _f64p, _f64p, _vp, _vp]),
+        "anacor_surrogate_set_data": (_int, [_vp, _f32p, _f64p, ct.c_int64]),
+        "anacor_surrogate_train": (_int, [_vp, _int, _int, ct.c_float, ct.c_float, _int, _vp]),
+        "anacor_surrogate_gradients": (_int, [_vp, _f32p, _f32p, _int, _vp, _vp]),
+        "anacor_surrogate_predict": (_int, [_vp, _f32p, ct.c_int64, _f32p, _f32p, _vp]),
+        "anacor_surrogate_predict_device": (_int, [_vp, _vp, ct.c_int64, _vp, _vp, _vp, _vp]),
+        "anacor_surrogate_audit_flags": (_int, [_vp, ct.c_int64, ct.c_uint32, ct.c_double, ct.c_float, _vp, _vp]),
+        "anacor_surrogate_save": (_int, [_vp, ct.c_char_p]),
+        "anacor_surrogate_load": (_int, [_vp, ct.c_char_p]),
+        "anacor_tc_gemm_check": (_int, [_f32p, _f32p, _int, _int, _int, _int, _int, _f32p]),
+    }
+    for name, (res, args) in sigs.items():
+        getattr(L, name).restype = res
+        getattr(L, name).argtypes = args
     L.free.restype = None
     L.free.argtypes = [ct.c_void_p]
     if path == _build.LIB:

@@ -45,8 +45,15 @@ WORKLOADS = {
     "small": "96^3 int8 volume, all crystal voxels, 300 reflections",
     "batch": "12 samples 128^3..640x640x480, 2k-60k reflections each, one persistent launch (CUDA graph)",
     "highabs": "1024x1024x800 int8 volume, all crystal voxels, mu x5, reflection subset of 50000",
+    "surrogate": "beamline sample; 4-member MLP ensemble trained on 100000 traced reflections (20000 Adam "
+                 "steps, batch 4096); inference on 1000000 fresh reflections, 2% random audit + spread>1e-3 "
+                 "re-traced by the plain kernel",
+    "highabs_surrogate": "1024x1024x800 high-absorption sample, all crystal voxels; ensemble trained as for "
+                         "the beamline sample; 50000 reflections with the 2% audit + spread fallback",
 }
-DEFAULT_REFL = {"beamline": 20000, "small": 300, "batch": 0, "highabs": 256}
+DEFAULT_REFL = {"beamline": 20000, "small": 300, "batch": 0, "highabs": 256, "surrogate": 1000000,
+                "highabs_surrogate": 50000}
+SURROGATE_METRIC = "reflections/s (surrogate with audit: ensemble A_h, 2% random + high-spread re-traced)"
 
 
 def parse():
@@ -61,6 +68,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--train-refl", type=int, default=100000, help="surrogate: traced training reflections")
+    ap.add_argument("--train-steps", type=int, default=20000, help="surrogate: Adam steps")
+    ap.add_argument("--train-batch", type=int, default=4096)
+    ap.add_argument("--members", type=int, default=4)
+    ap.add_argument("--fourier-scale", type=float, default=1.0)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--audit", type=float, default=0.02)
+    ap.add_argument("--spread", type=float, default=1e-3)
     a = ap.parse_args()
     if a.refl is None:
         a.refl = DEFAULT_REFL[a.workload]
@@ -80,6 +95,10 @@ def make_samples(args, rank: int = 0):
         ss = [synth.small_sample(n_refl=args.refl)]
     elif w == "highabs":
         ss = [synth.high_absorption_sample(n_refl=args.refl)]
+    elif w == "surrogate":
+        ss = [synth.beamline_sample()]
+    elif w == "highabs_surrogate":
+        ss = [synth.high_absorption_sample(n_refl=256)]
     else:
         ss = synth.batch_samples(n_samples=12)
     if rank > 0:
@@ -423,10 +442,217 @@ def e2e_dropin(L, samples, steps, torch):
             "checksum": checksum}
 
 
+def _quantiles(e):
+    e = np.asarray(e, dtype=np.float64)
+    if e.size == 0:
+        return None
+    return {"n": int(e.size), "median": float(np.median(e)), "p90": float(np.quantile(e, 0.9)),
+            "p99": float(np.quantile(e, 0.99)), "max": float(e.max())}
+
+
+def run_surrogate(args):
+    """Surrogate with audit on one sample: trace a training set with the plain
+    kernel, train the ensemble, then time inference over fresh reflections with
+    the audit rows and the high-spread rows re-traced."""
+    import ctypes as ct
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from anacor_public_gb300 import _lib, build, surrogate, synth, tracer
+    build.build()
+    L = _lib.load()
+    s = make_samples(args, rank)[0]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    plan = tracer.Plan(s.label, s.coords, s.voxel, s.mu)
+    plan.set_reflections(s.s1, s.omega, s.xray, s.omega_axis, s.F)
+    if not args.no_autotune:
+        plan.autotune()
+    tuned = plan.config()
+
+    # training set traced by the plain kernel (its throughput is the plain reference point)
+    rng = np.random.default_rng(17 + rank)
+    om_t, s1_t = synth.reflections(args.train_refl, rng, xray=s.xray)
+    plan.set_reflections(s1_t, om_t, s.xray, s.omega_axis, s.F)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plan.run(sh)
+    e1.record(stream)
+    ah_t = plan.result(sh)
+    trace_ms = e0.elapsed_time(e1)
+    plain_rate = args.train_refl / (trace_ms / 1e3)
+    x7_t = surrogate.inputs(om_t, s1_t, s.xray, s.omega_axis, s.F)
+    model = surrogate.Surrogate(members=args.members, seed=1 + rank, fourier_scale=args.fourier_scale)
+    model.set_data(x7_t, np.log(ah_t))
+    t0 = time.perf_counter()
+    loss = model.train(args.train_steps, batch=args.train_batch, lr_max=args.lr, lr_min=args.lr * 1e-2,
+                       total_steps=args.train_steps)
+    train_s = time.perf_counter() - t0
+
+    # fresh reflections, resident on the device
+    n = args.refl
+    om_i, s1_i = synth.reflections(n, np.random.default_rng(1000 + rank), xray=s.xray)
+    d_om = torch.from_numpy(om_i).to("cuda")
+    d_s1 = torch.from_numpy(s1_i).to("cuda")
+    d_x7 = torch.empty((n, 7), dtype=torch.float32, device="cuda")
+    d_mean = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_spread = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_flags = torch.empty(n, dtype=torch.uint8, device="cuda")
+    d_out = torch.empty(n, dtype=torch.float64, device="cuda")
+    geo = (np.ascontiguousarray(s.xray, dtype=np.float64), np.ascontiguousarray(s.omega_axis, dtype=np.float64),
+           np.ascontiguousarray(s.F, dtype=np.float64).reshape(-1))
+    record = {}
+
+    def step(k, host=None):
+        if host is not None:   # e2e: this step's inputs arrive from pinned host memory
+            d_om.copy_(host[0], non_blocking=True)
+            d_s1.copy_(host[1], non_blocking=True)
+        _lib.check(L.anacor_surrogate_inputs_device(ct.c_void_p(d_om.data_ptr()), ct.c_void_p(d_s1.data_ptr()), n,
+                                                    *geo, ct.c_void_p(d_x7.data_ptr()), ct.c_void_p(sh)), L)
+        model.predict_device(d_x7.data_ptr(), n, d_mean.data_ptr(), d_spread.data_ptr(), sh)
+        surrogate.audit_flags(d_spread.data_ptr(), n, 100 + k, args.audit, args.spread, d_flags.data_ptr(), sh)
+        d_out.copy_(d_mean)
+        flags = d_flags.cpu().numpy()            # synchronises the stream
+        idx = np.nonzero(flags)[0]
+        if idx.size:
+            plan.set_reflections(s1_i[idx], om_i[idx], s.xray, s.omega_axis, s.F)
+            plan.run(sh)
+            traced = torch.from_numpy(plan.result(sh)).to("cuda", non_blocking=True)
+            d_out.index_copy_(0, torch.from_numpy(idx).to("cuda", non_blocking=True), traced)
+        else:
+            traced = None
+        record.update(flags=flags, idx=idx, traced=traced)
+        if host is not None:
+            host[2].copy_(d_out, non_blocking=True)
+        return idx.size
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    # accuracy of this pass (the audit rows: surrogate vs traced)
+    err_sur, err_out, fallback, n_traced = [], [], [], []
+
+    def account():
+        fl, idx = record["flags"], record["idx"]
+        tr = record["traced"].cpu().numpy() if record["traced"] is not None else np.zeros(0)
+        mean = d_mean.cpu().numpy().astype(np.float64)
+        aud = (fl[idx] & 1) != 0
+        e = np.abs(mean[idx[aud]] - tr[aud]) / np.abs(tr[aud])
+        err_sur.append(e)
+        err_out.append(np.where((fl[idx[aud]] & 2) != 0, 0.0, e))   # fallback rows leave the output exact
+        fallback.append(float(np.mean((fl & 2) != 0)))
+        n_traced.append(int(idx.size))
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms = []
+    for k in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(args.warmup + k)
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+        account()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms_step = sum(ms) / len(ms)
+    if world > 1:
+        t = torch.tensor([ms_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = n * world / (ms_step / 1e3)
+
+    # the network alone: inputs + ensemble inference over the n rows
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush.zero_()
+    a.record(stream)
+    model.predict_device(d_x7.data_ptr(), n, d_mean.data_ptr(), d_spread.data_ptr(), sh)
+    b.record(stream)
+    b.synchronize()
+    infer_ms = a.elapsed_time(b)
+    flops_row = 2 * (64 * 256 + 3 * 256 * 256 + 256) * args.members
+    tflops = flops_row * n / (infer_ms / 1e3) / 1e12
+
+    e2e = None
+    if not args.no_e2e:
+        h_om = torch.from_numpy(om_i).pin_memory()
+        h_s1 = torch.from_numpy(s1_i).pin_memory()
+        h_out = torch.empty(n, dtype=torch.float64).pin_memory()
+        tt = []
+        for k in range(args.steps + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step(500 + k, host=(h_om, h_s1, h_out))
+            stream.synchronize()
+            if k:
+                tt.append(time.perf_counter() - t0)
+        e2e = {"value": n / (sum(tt) / len(tt)), "unit": "reflections/s",
+               "h2d_bytes_per_step": int(n * 32), "d2h_bytes_per_step": int(n * 9),
+               "path": "surrogate.audited pipeline from pinned host omega / s1 to host A_h"}
+        if world > 1:
+            t = torch.tensor([sum(tt) / len(tt)], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e["value"] = n * world / float(t.item())
+
+    if rank == 0:
+        peak_tf = None
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            with open(pk) as f:
+                peak_tf = float(json.load(f).get("bf16_tflops", 0)) or None
+        cpu = None if args.no_cpu_baseline else cpu_baseline([s], args.cpu_seconds)
+        es, eo = np.concatenate(err_sur), np.concatenate(err_out)
+        line = {
+            "metric": SURROGATE_METRIC, "value": value, "unit": "reflections/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload], "n_voxels": len(s.coords), "n_reflections": n,
+                       "volume": list(s.label.shape), "members": args.members, "train_refl": args.train_refl,
+                       "train_steps": args.train_steps, "train_batch": args.train_batch,
+                       "audit_fraction": args.audit, "spread_threshold": args.spread,
+                       "l2": "flushed between steps (256 MiB write)", "tuned": tuned},
+            "plain_refl_per_s": plain_rate,
+            "speedup_vs_plain": value / plain_rate,
+            "surrogate": {"train_s": train_s, "train_trace_s": trace_ms / 1e3,
+                          "final_loss": float(np.mean(loss[-100:])), "first_loss": float(np.mean(loss[:10])),
+                          "fallback_fraction": float(np.mean(fallback)), "traced_per_step": int(np.mean(n_traced)),
+                          "surrogate_rel_err": _quantiles(es), "output_rel_err": _quantiles(eo),
+                          "inference_ms": infer_ms, "inference_tflops": tflops},
+            "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak_tf, "unit": "TFLOP/s",
+                         "frac": (tflops / peak_tf) if peak_tf else None, "traffic": None,
+                         "kernel": "ensemble inference (tcgen05 GEMMs + fused bias/GELU epilogues)"},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clk,
+            # per step: inputs, per 262144-row chunk features + 4 GEMMs + head + ensemble,
+            # audit flags, the absorption launch(es) of the traced rows
+            "gpu_launches": args.steps * (2 + 7 * (-(-n // 262144)) + plan.launch_info()[1]),
+        }
+        print(json.dumps(line), flush=True)
+    model.close()
+    plan.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in ("surrogate", "highabs_surrogate"):
+        run_surrogate(args)
     else:
         run_ours(args)
 

@@ -194,6 +194,69 @@ int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *shape, const
                               const double *voxel, const double *mu, int full_iteration, int is_exp,
                               double *d_out, void *stream);
 
+/* ------------------------------------------------------ learned surrogate -- */
+
+/* No counterpart in the reference (its absorption factors always come from
+ * the ray tracer).  An ensemble of MLPs per sample: x7 = (omega / 2pi wrapped
+ * to [0, 1), incident and diffracted unit vectors in the crystal frame) ->
+ * 64 Fourier features [sin 2pi(Bx), cos 2pi(Bx)] -> 4 x 256 GELU -> the
+ * standardised log A_h.  BF16 weights and activations, FP32 accumulation on
+ * the tcgen05 tensor cores, FP32 Adam masters.  Training targets are absorption
+ * factors computed by the tracer; at inference the ensemble spread flags the
+ * reflections to re-trace.  Calls run on the object's own stream unless a
+ * stream is passed, and are not thread-safe on one object. */
+typedef struct anacor_surrogate anacor_surrogate;
+
+anacor_surrogate *anacor_surrogate_create(int n_members, uint32_t seed, float fourier_scale);
+void anacor_surrogate_destroy(anacor_surrogate *s);
+/* FP32 parameters per member (layers 1-4 weights [out][in] and biases, then
+ * the output weights and bias, padded to a multiple of 8) */
+int64_t anacor_surrogate_param_count(void);
+int anacor_surrogate_members(const anacor_surrogate *s);
+/* copy all members' parameters [members][param_count] to (to_device = 0) or
+ * from (1) host memory */
+int anacor_surrogate_params(anacor_surrogate *s, float *host, int to_device);
+/* the 32 x 7 Fourier matrix B, read (0) or written (1) */
+int anacor_surrogate_fourier(anacor_surrogate *s, float *host32x7, int to_device);
+/* output scale: log A_h = mean + std_dev * y; read (set = 0) or written */
+int anacor_surrogate_scale(anacor_surrogate *s, double *mean, double *std_dev, int set);
+/* x7 rows [n][7] of reflections (omega, s1 as for anacor_absorption) */
+int anacor_surrogate_inputs(const double *omega, const double *s1, int64_t n, const double *xray,
+                            const double *omega_axis, const double *F, float *x7_out);
+int anacor_surrogate_inputs_device(const double *d_omega, const double *d_s1, int64_t n, const double *xray,
+                                   const double *omega_axis, const double *F, float *d_x7, void *stream);
+/* training set: n rows of x7 and their log A_h; sets the output scale to the
+ * targets' mean and standard deviation */
+int anacor_surrogate_set_data(anacor_surrogate *s, const float *x7, const double *log_ah, int64_t n);
+/* `steps` Adam steps; each member draws its own batch of `batch` rows (a
+ * multiple of 1024) with replacement.  The learning rate follows a cosine
+ * from lr_max to lr_min over total_steps (counted from the first step ever
+ * taken).  loss_out (optional, `steps` floats): mean member loss per step. */
+int anacor_surrogate_train(anacor_surrogate *s, int steps, int batch, float lr_max, float lr_min, int total_steps,
+                           float *loss_out);
+/* gradients of every member's loss on one batch (rows a multiple of 1024;
+ * targets in output units y), without an update: grads_out [members][param
+ * count] (optional), y_out [members][rows] (optional) */
+int anacor_surrogate_gradients(anacor_surrogate *s, const float *x7, const float *target, int rows,
+                               float *grads_out, float *y_out);
+/* ensemble mean of A_h and relative spread (std / mean over members) for n
+ * rows of x7; members_out (optional) [members][n] log A_h per member */
+int anacor_surrogate_predict(anacor_surrogate *s, const float *x7, int64_t n, float *mean_out, float *spread_out,
+                             float *members_out);
+int anacor_surrogate_predict_device(anacor_surrogate *s, const float *d_x7, int64_t n, float *d_mean,
+                                    float *d_spread, float *d_members, void *stream);
+/* flags[i] bit 0: row i is in the seeded random audit sample (probability
+ * audit_fraction); bit 1: spread[i] > spread_threshold or not finite */
+int anacor_surrogate_audit_flags(const float *d_spread, int64_t n, uint32_t seed, double audit_fraction,
+                                 float spread_threshold, uint8_t *d_flags, void *stream);
+int anacor_surrogate_save(anacor_surrogate *s, const char *path);
+int anacor_surrogate_load(anacor_surrogate *s, const char *path);
+
+/* the surrogate's tensor-core GEMM alone, for checks: C[z] = A[z] B[z]^T with
+ * A [batch][M][K], B [batch][N][K] rounded to BF16, FP32 accumulation, the K
+ * range split into ksplit slices whose partial products are summed in order */
+int anacor_tc_gemm_check(const float *A, const float *B, int M, int N, int K, int batch, int ksplit, float *C);
+
 /* ---------------------------------------------------------- diagnostics -- */
 
 /* Rotated incident and diffracted vectors of n reflections, computed by the

@@ -37,6 +37,10 @@ EXPORTS = (
     "anacor_surrogate_train", "anacor_surrogate_gradients", "anacor_surrogate_predict",
     "anacor_surrogate_predict_device", "anacor_surrogate_audit_flags", "anacor_surrogate_save",
     "anacor_surrogate_load", "anacor_tc_gemm_check",
+    "anacor_gridding_directions", "anacor_gridding_create", "anacor_gridding_build", "anacor_gridding_info",
+    "anacor_gridding_axes", "anacor_gridding_device_map", "anacor_gridding_map", "anacor_gridding_set_map",
+    "anacor_gridding_interpolate", "anacor_gridding_interpolate_async", "anacor_gridding_destroy",
+    "ray_tracing_single_gridding", "ib_single_gridding", "nearest_neighbor_interpolate_overall",
 )
 
 _LIB = None
@@ -171,6 +175,41 @@ def load(path: str | None = None) -> ct.CDLL:
         "anacor_surrogate_load": (_int, [_vp, ct.c_char_p]),
         "anacor_tc_gemm_check": (_int, [_f32p, _f32p, _int, _int, _int, _int, _int, _f32p]),
     }
+    # gridding (absorption map)
+    sigs.update({
+        "anacor_gridding_directions": (_int, [_int, _int, _f64p, _f64p, _f64p]),
+        "anacor_gridding_create": (_vp, [_vp, _int, _int, _int]),
+        "anacor_gridding_build": (_int, [_vp, _vp, _vp, _vp]),
+        "anacor_gridding_info": (_int, [_vp, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64), ct.POINTER(_int),
+                                        ct.POINTER(_int)]),
+        "anacor_gridding_axes": (_int, [_vp, _f64p, _f64p]),
+        "anacor_gridding_device_map": (_vp, [_vp, ct.POINTER(ct.c_int64)]),
+        "anacor_gridding_map": (_int, [_vp, _f32p]),
+        "anacor_gridding_set_map": (_int, [_vp, _f32p]),
+        "anacor_gridding_interpolate": (_int, [_vp, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p, _int, _f64p]),
+        "anacor_gridding_interpolate_async": (_int, [_vp, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p, _int,
+                                                     _vp, _vp]),
+        "anacor_gridding_destroy": (None, [_vp]),
+        # drop-ins, argtypes as AnACor/utils/utils_gridding.py:104-134 and :547-573
+        "ray_tracing_single_gridding": (ct.c_double, [np.ctypeslib.ndpointer(dtype=np.int64),
+                                                      np.ctypeslib.ndpointer(dtype=np.float64), ct.c_double,
+                                                      ct.c_double, np.ctypeslib.ndpointer(dtype=np.float64),
+                                                      np.ctypeslib.ndpointer(dtype=np.float64), _i8ppp,
+                                                      np.ctypeslib.ndpointer(dtype=np.int64), _int, _int, _int]),
+        "ib_single_gridding": (ct.c_double, [np.ctypeslib.ndpointer(dtype=np.int64),
+                                             np.ctypeslib.ndpointer(dtype=np.float64), ct.c_double, ct.c_double,
+                                             np.ctypeslib.ndpointer(dtype=np.float64),
+                                             np.ctypeslib.ndpointer(dtype=np.float64), _i8ppp,
+                                             np.ctypeslib.ndpointer(dtype=np.int64), _int, _int, _int, _int]),
+        "nearest_neighbor_interpolate_overall": (ct.POINTER(ct.c_double), [
+            ct.c_int64, ct.c_int64, np.ctypeslib.ndpointer(dtype=np.int64), ct.c_int64,
+            np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64),
+            np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64),
+            np.ctypeslib.ndpointer(dtype=np.float64), ct.c_int64, np.ctypeslib.ndpointer(dtype=np.float64),
+            np.ctypeslib.ndpointer(dtype=np.float64), _int, _int, np.ctypeslib.ndpointer(dtype=np.float64),
+            np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64), ct.c_int64,
+            ct.c_int64, ct.c_double, ct.c_double, ct.c_double, ct.c_double, _int]),
+    })
     for name, (res, args) in sigs.items():
         getattr(L, name).restype = res
         getattr(L, name).argtypes = args

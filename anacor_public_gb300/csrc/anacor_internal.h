@@ -85,6 +85,15 @@ int setup_reflection(const double *omega_axis, double omega, const double *F, co
                      const double *s1, ReflTable *out, double *rotated_xray, double *rotated_s1);
 // Set-up from already rotated vectors (ray_tracing_single's inputs).
 int setup_rotated(const double *rotated_xray, const double *rotated_s1, ReflTable *out);
+// Diffracted leg only (leg 0 zeroed) of a direction whose polar angles are
+// given, as ray_tracing_single_gridding takes them
+// (AnACor/src/ray_tracing.c:484-534).
+int setup_direction(const double *rotated_s1, double theta, double phi, ReflTable *out);
+// dials_2_thetaphi_22 (AnACor/src/ray_tracing_basic.c:13-50); incident legs use -v.
+void polar_angles(const double *v, bool incident, double *theta, double *phi);
+// Rotated incident and diffracted vectors of one reflection (matrices.h:49-68 order).
+void rotate_reflection(const double *omega_axis, double omega, const double *F, const double *xray,
+                       const double *s1, double *rotated_xray, double *rotated_s1);
 // OpenMP-parallel set-up of many reflections; returns the first error status.
 int setup_reflections(const double *omega_axis, const double *omega, const double *F, const double *xray,
                       const double *s1, int64_t n, ReflTable *out, int threads);

@@ -593,6 +593,34 @@ int batch_check(anacor_batch *b, cudaStream_t st)
 
 }  // namespace
 
+namespace anacor {
+int plan_view(const anacor_plan *p, PlanView *v)
+{
+    if (!p || !v)
+        return fail(kErrArgs, "null plan");
+    std::memset(v, 0, sizeof(*v));
+    v->vol = p->d_vol;
+    for (int a = 0; a < 3; a++) {
+        v->dims[a] = p->dims[a];
+        v->voxel[a] = p->voxel[a];
+    }
+    for (int a = 0; a < 4; a++)
+        v->mu[a] = p->mu[a];
+    v->n_vox = p->n_vox;
+    v->coords = p->d_coords;
+    v->c64 = p->d_c64;
+    v->morton = p->morton ? 1 : 0;
+    v->full_iteration = p->full;
+    v->is_exp = p->is_exp;
+    v->sq = p->d_sq;
+    v->sq_stride = p->sq_stride;
+    v->qtab = p->d_qtab;
+    v->stream = p->stream;
+    v->sms = p->dev ? p->dev->sms : 0;
+    return kOk;
+}
+}  // namespace anacor
+
 extern "C" {
 
 int anacor_last_status(void) { return t_status; }

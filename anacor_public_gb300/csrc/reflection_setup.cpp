@@ -224,10 +224,23 @@ int setup_rotated(const double *xr, const double *sr, ReflTable *out)
     return fill_leg(d_out, false, th_out, ph_out, out->head[1], out->rule[1]);
 }
 
-int setup_reflection(const double *axis, double omega, const double *F, const double *xray,
-                     const double *s1, ReflTable *out, double *rx, double *rs)
+int setup_direction(const double *sr, double theta, double phi, ReflTable *out)
 {
-    double r[9], rf[9], t[9], xr[3], sr[3];
+    std::memset(out, 0, sizeof(*out));
+    double d_out[3];
+    my_frame(sr, d_out);
+    return fill_leg(d_out, false, theta, phi, out->head[1], out->rule[1]);
+}
+
+void polar_angles(const double *v, bool incident, double *theta, double *phi)
+{
+    polar(v, incident, *theta, *phi);
+}
+
+void rotate_reflection(const double *axis, double omega, const double *F, const double *xray, const double *s1,
+                       double *xr, double *sr)
+{
+    double r[9], rf[9], t[9];
     rotation_about(axis, omega, r);
     product(r, F, rf, 3, 3, 3);
     for (int i = 0; i < 3; i++)
@@ -235,6 +248,13 @@ int setup_reflection(const double *axis, double omega, const double *F, const do
             t[j * 3 + i] = rf[i * 3 + j];
     product(t, xray, xr, 3, 3, 1);
     product(t, s1, sr, 3, 3, 1);
+}
+
+int setup_reflection(const double *axis, double omega, const double *F, const double *xray,
+                     const double *s1, ReflTable *out, double *rx, double *rs)
+{
+    double xr[3], sr[3];
+    rotate_reflection(axis, omega, F, xray, s1, xr, sr);
     if (rx)
         std::memcpy(rx, xr, sizeof(xr));
     if (rs)

@@ -35,6 +35,7 @@
 #include <cstdlib>
 
 #include "anacor_internal.h"
+#include "device_math.cuh"
 #include "trace_launch.h"
 
 namespace anacor {
@@ -576,23 +577,6 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
     }
 }
 
-// exp(-x) in FP32 after an FP64 reduction x = k ln2 + r, |r| <= ln2/2.
-__device__ __forceinline__ float exp_neg(double x)
-{
-    const double kd = rint(__dmul_rn(x, 1.4426950408889634));
-    const double r = __fma_rn(-kd, 0.6931471805599453, x);
-    const float e = expf(-(float)r);
-    const int k = (int)fmaxf(fminf((float)kd, 400.0f), -400.0f);
-    return ldexpf(e, -k);
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-    s = a + b;
-    const float bp = s - a;
-    e = (a - (s - bp)) + (b - bp);
-}
-
 __device__ __forceinline__ int find_sample(const SampleDesc *d, int n, long long item)
 {
     int s = 0;
@@ -727,6 +711,71 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
                 D.arrive[r] = 0u;   // ready for the next launch
             }
         }
+    }
+}
+
+// Absorption map: work item = (grid direction, tile of voxels); the
+// diffracted leg of every voxel, one output per (direction, voxel).
+__global__ void __launch_bounds__(kBlock, 2) gridding_map_kernel(const MapDesc *__restrict__ dp, long long total_items,
+                                                                 unsigned long long *__restrict__ work_counter)
+{
+    __shared__ ReflTable tab;
+    __shared__ uint16_t seg[kMaxSegments * kBlock];
+    __shared__ long long item_s;
+    const MapDesc &D = *dp;
+    const int tid = threadIdx.x;
+    const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2]};
+    for (;;) {
+        if (tid == 0)
+            item_s = (long long)atomicAdd(work_counter, 1ull);
+        __syncthreads();
+        const long long item = item_s;
+        if (item >= total_items)
+            break;
+        const long long d = item / D.tiles;
+        const int t = (int)(item - d * D.tiles);
+        {
+            const int4 *src = reinterpret_cast<const int4 *>(D.dirs + d);
+            int4 *dst = reinterpret_cast<int4 *>(&tab);
+            for (int k = tid; k < (int)(sizeof(ReflTable) / 16); k += kBlock)
+                dst[k] = __ldg(src + k);
+        }
+        __syncthreads();
+        int bad = kOk;
+        const int v0 = t * D.tile;
+        const int v1 = min(D.n_vox, v0 + D.tile);
+        float *row = D.out + d * D.ld;
+        for (int vb = v0; vb < v1; vb += kBlock) {
+            const int vi = vb + tid;
+            const bool valid = vi < v1;
+            const short4 cv = valid ? __ldg(D.coords + vi) : make_short4(0, 0, 0, 0);
+            LegResult a;
+            trace_leg<false>(tab.head[1], tab.rule[1], cv.x, cv.y, cv.z, valid, v, D.full_iteration, D.voxel,
+                             D.sq, D.sq_stride, D.qtab, seg + tid, a);
+            if (!valid)
+                continue;
+            double val;
+            if (a.status) {
+                bad |= a.status;
+                val = __longlong_as_double(0x7ff8000000000000ll);
+            } else {
+                // cal_rate with a zero incident leg: (0 + L) == L per class
+                const double t0 = __dmul_rn(D.mu[0], a.L[0]);
+                const double t1 = __dmul_rn(D.mu[1], a.L[1]);
+                const double t2 = __dmul_rn(D.mu[2], a.L[2]);
+                const double t3 = __dmul_rn(D.mu[3], a.L[3]);
+                const double ex = __dadd_rn(__dadd_rn(__dadd_rn(t0, t1), t2), t3);
+                val = D.is_exp ? exp(-ex) : ex;
+            }
+            const long long o = D.col ? __ldg(D.col + vi) : vi;
+            if (D.out64)
+                D.out64[d * D.ld + o] = val;
+            else
+                row[o] = (float)val;
+        }
+        if (bad)
+            atomicOr(D.status, 1 << bad);
+        __syncthreads();   // the table and item_s are rewritten next
     }
 }
 
@@ -883,6 +932,25 @@ cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const
                                                                     d_coords, n, d_voxel, full, d_sq, sq_stride,
                                                                     d_qtab, face, len, nseg, first, last, L, status);
     return cudaGetLastError();
+}
+
+cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,
+                                cudaStream_t st)
+{
+    if (total_items <= 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess)
+        return e;
+    gridding_map_kernel<<<grid, kBlock, 0, st>>>(d_desc, total_items, d_counter);
+    return cudaGetLastError();
+}
+
+int gridding_map_occupancy(int *blocks_per_sm)
+{
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gridding_map_kernel, kBlock, 0) == cudaSuccess
+               ? kOk
+               : kErrCuda;
 }
 
 int absorption_block_threads() { return kBlock; }

@@ -5,6 +5,8 @@
 
 #include "anacor_internal.h"
 
+struct anacor_plan;
+
 namespace anacor {
 
 // Voxels per work item (one CTA pass) unless a sample sets its own: a sample
@@ -38,6 +40,50 @@ struct SampleDesc {
     long long work_begin;   // first global work item of this sample
 };
 
+// Absorption map of one sample (gridding mode): for every grid direction d and
+// voxel k the diffracted leg alone, out[d * ld + k] = (float) sum_m mu_m L_m
+// (or (float) exp(-sum) when is_exp), as ray_tracing_single_gridding computes
+// it (AnACor/src/ray_tracing.c:484-534) with cal_rate's zero incident leg.
+struct MapDesc {
+    const int8_t *vol;
+    int dim[3];
+    int n_vox;
+    const short4 *coords;
+    const ReflTable *dirs;  // [n_dirs], leg 1 set
+    long long n_dirs;
+    int tiles, tile;
+    int full_iteration;
+    int is_exp;
+    double mu[4];
+    double voxel[3];
+    float *out;
+    double *out64;          // optional: the FP64 values instead (out unused)
+    long long ld;
+    const int *col;         // optional: output column of packed voxel k
+    int *status;
+    const double *sq;
+    int sq_stride;
+    const double *qtab;
+};
+
+// Device-resident sample of a plan, for the other entry points that march it.
+struct PlanView {
+    const int8_t *vol;
+    int dims[3];
+    int n_vox;
+    const short4 *coords;     // packed list (Morton order when morton)
+    const long long *c64;     // the caller's (z, y, x) list, device
+    int morton;
+    int full_iteration, is_exp;
+    double mu[4], voxel[3];
+    const double *sq;
+    int sq_stride;
+    const double *qtab;
+    cudaStream_t stream;
+    int sms;
+};
+int plan_view(const anacor_plan *p, PlanView *out);
+
 int rcp_table_init();
 int absorption_block_threads();
 // CTAs per SM of a register-budget variant (1..4; 0 = the process default)
@@ -50,6 +96,8 @@ cudaError_t launch_pack_coords(const long long *d_c, int n, const int *dims, sho
 // Same, with the packed list sorted by the Morton code of (z, y, x).
 cudaError_t launch_pack_coords_morton(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
                                       cudaStream_t st);
+// perm[k] = index in the caller's list of the k-th voxel of the Morton-packed list
+cudaError_t launch_morton_permutation(const long long *d_c, int n, const int *dims, int *d_perm, cudaStream_t st);
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs
 // take items from `d_counter` (reset inside the launch sequence).
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,
@@ -58,6 +106,26 @@ cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const
                               int n, const double *d_voxel, int full, const double *d_sq, int sq_stride,
                               const double *d_qtab, int *face, int *len, int *nseg, int *first, int *last, double *L,
                               int *status, cudaStream_t st);
+// Persistent launch over n_dirs * tiles work items of the map.
+cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,
+                                cudaStream_t st);
+int gridding_map_occupancy(int *blocks_per_sm);
+// Lookup of one reflection in an absorption map: for each leg (0 incident,
+// 1 diffracted) the map rows (grid directions) and weights of the value, as
+// the reference's interpolation reads it
+// (AnACor/src/gridding_interpolation.c:16-45, 48-76): nearest uses row[l][0];
+// bilinear sums w[l][j] * z(row[l][j]) for j = 0..3 in that order.
+struct InterpRow {
+    long long row[2][4];
+    double w[2][4];
+};
+// out[r] = mean over voxels k of exp(-(z_0 + z_1)), z_l the leg's map value;
+// value (k, row) is map[k * sK + row * sR]
+cudaError_t launch_gridding_interp_f32(const float *map, long long sK, long long sR, int n_vox, const InterpRow *rows,
+                                       long long n_refl, int linear, double *out, cudaStream_t st);
+cudaError_t launch_gridding_interp_f64(const double *map, long long sK, long long sR, int n_vox,
+                                       const InterpRow *rows, long long n_refl, int linear, double *out,
+                                       cudaStream_t st);
 // Table of correctly rounded quotients fl(s / d), 1 <= d <= max_den,
 // 1 <= s <= d + 1 (row d starts at (d-1)(d+2)/2).
 size_t quotient_table_entries(int max_den);

@@ -46,7 +46,51 @@ __global__ void pack_keys_kernel(const long long *__restrict__ c, int n, int dz,
     vals[i] = *reinterpret_cast<const unsigned long long *>(&p);
 }
 
+__global__ void index_keys_kernel(const long long *__restrict__ c, int n, int dz, int dy, int dx,
+                                  unsigned long long *__restrict__ keys, int *__restrict__ idx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    long long z = c[3 * i], y = c[3 * i + 1], x = c[3 * i + 2];
+    if (z < 0 || z >= dz || y < 0 || y >= dy || x < 0 || x >= dx)
+        z = y = x = 0;
+    keys[i] = (spread3((unsigned)z) << 2) | (spread3((unsigned)y) << 1) | spread3((unsigned)x);
+    idx[i] = i;
+}
+
 }  // namespace
+
+cudaError_t launch_morton_permutation(const long long *d_c, int n, const int *dims, int *d_perm, cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    unsigned long long *keys = nullptr;
+    int *idx = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    cudaError_t e;
+    if ((e = cudaMallocAsync(&keys, 2 * sizeof(unsigned long long) * (size_t)n, st)))
+        return e;
+    if ((e = cudaMallocAsync(&idx, sizeof(int) * (size_t)n, st))) {
+        cudaFreeAsync(keys, st);
+        return e;
+    }
+    index_keys_kernel<<<(n + 255) / 256, 256, 0, st>>>(d_c, n, dims[0], dims[1], dims[2], keys, idx);
+    e = cudaGetLastError();
+    // the same keys, bit range and stable sort as launch_pack_coords_morton
+    if (!e)
+        e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys + n, idx, d_perm, n, 0, 39, st);
+    if (!e)
+        e = cudaMallocAsync(&tmp, tmp_bytes, st);
+    if (!e)
+        e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys + n, idx, d_perm, n, 0, 39, st);
+    if (tmp)
+        cudaFreeAsync(tmp, st);
+    cudaFreeAsync(keys, st);
+    cudaFreeAsync(idx, st);
+    return e;
+}
 
 cudaError_t launch_pack_coords_morton(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
                                       cudaStream_t st)

@@ -62,7 +62,7 @@ def tc_gemm(A: np.ndarray, B: np.ndarray, ksplit: int = 1) -> np.ndarray:
 class Surrogate:
     """Ensemble of ``members`` networks living on the current CUDA device."""
 
-    def __init__(self, members: int = 4, seed: int = 0, fourier_scale: float = 1.0):
+    def __init__(self, members: int = 4, seed: int = 0, fourier_scale: float = 0.5):
         self._L = _lib.load()
         h = self._L.anacor_surrogate_create(int(members), int(seed) & 0xFFFFFFFF, float(fourier_scale))
         if not h:
@@ -106,7 +106,7 @@ class Surrogate:
         x7 = _c(x7, np.float32).reshape(-1, 7)
         _lib.check(self._L.anacor_surrogate_set_data(self._h, x7, _c(log_ah, np.float64), x7.shape[0]), self._L)
 
-    def train(self, steps: int, batch: int = 4096, lr_max: float = 1e-3, lr_min: float = 1e-5,
+    def train(self, steps: int, batch: int = 4096, lr_max: float = 3e-3, lr_min: float = 3e-5,
               total_steps: int | None = None) -> np.ndarray:
         """Adam steps on the training set; returns the mean member loss of each step."""
         loss = np.zeros(max(steps, 1), dtype=np.float32)
@@ -251,8 +251,8 @@ def audited_absorption(model: Surrogate, plan: tracer.Plan, omega, s1, xray, ome
 
 
 def train_for_sample(s: synth.Sample, n_train: int = 100_000, steps: int = 20_000, batch: int = 4096,
-                     members: int = 4, seed: int = 0, fourier_scale: float = 1.0, lr_max: float = 1e-3,
-                     lr_min: float = 1e-5, plan: tracer.Plan | None = None):
+                     members: int = 4, seed: int = 0, fourier_scale: float = 0.5, lr_max: float = 3e-3,
+                     lr_min: float = 3e-5, plan: tracer.Plan | None = None):
     """Trace a training set on the sample and train an ensemble on it; returns
     (model, loss history)."""
     omega, s1, ah = training_set(s, n_train, seed=seed + 7, plan=plan)

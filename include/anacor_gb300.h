@@ -194,6 +194,73 @@ int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *shape, const
                               const double *voxel, const double *mu, int full_iteration, int is_exp,
                               double *d_out, void *stream);
 
+/* ------------------------------------------------ gridding (absorption map) -- */
+
+/* The reference's approximate mode (AnACor/utils/utils_gridding.py:63-473):
+ * a map of the diffracted leg alone for every direction of a regular
+ * (theta, phi) grid and every crystal voxel, then per reflection a lookup of
+ * both legs' map values and A_h = mean_k exp(-(z_incident + z_diffracted)).
+ * The map stays on the GPU ([direction][voxel], the plan's voxel order);
+ * the object borrows the plan, which must outlive it. */
+typedef struct anacor_gridding anacor_gridding;
+
+/* Grid direction i = i_phi * n_theta + i_theta (utils_gridding.py:270-276 and
+ * :140-152): its DIALS-frame unit vector [3] and polar angles. */
+int anacor_gridding_directions(int n_theta, int n_phi, double *rotated_s1, double *theta, double *phi);
+/* method 2 (the reference's default): map = float32 sum_m mu_m L_m; method 1:
+ * float32 exp(-sum).  n_theta, n_phi >= 18 (the reference uses 360 x 180). */
+anacor_gridding *anacor_gridding_create(anacor_plan *plan, int n_theta, int n_phi, int method);
+/* Build the map.  With NULL arrays the directions are those of
+ * anacor_gridding_directions; otherwise the caller's per-direction vector and
+ * angles, as ray_tracing_single_gridding takes them. */
+int anacor_gridding_build(anacor_gridding *g, const double *rotated_s1, const double *theta, const double *phi);
+int anacor_gridding_info(const anacor_gridding *g, int64_t *n_dirs, int64_t *n_vox, int *len_theta, int *len_phi);
+/* the padded interpolation axes (utils_gridding.py:408-440), radians */
+int anacor_gridding_axes(const anacor_gridding *g, double *theta_axis, double *phi_axis);
+const float *anacor_gridding_device_map(const anacor_gridding *g, int64_t *ld);
+/* host copy / replacement of the map, [n_dirs][n_vox] in the caller's voxel
+ * order (the reference's saved absorption_map layout) */
+int anacor_gridding_map(const anacor_gridding *g, float *host_map);
+int anacor_gridding_set_map(anacor_gridding *g, const float *host_map);
+/* A_h of n reflections (omega, s1 as for anacor_absorption): method 1
+ * nearest grid point (the reference's default), 2 bilinear */
+int anacor_gridding_interpolate(anacor_gridding *g, const double *s1, const double *omega, int64_t n,
+                                const double *xray, const double *omega_axis, const double *F, int method,
+                                double *out);
+int anacor_gridding_interpolate_async(anacor_gridding *g, const double *s1, const double *omega, int64_t n,
+                                      const double *xray, const double *omega_axis, const double *F, int method,
+                                      double *d_out, void *stream);
+void anacor_gridding_destroy(anacor_gridding *g);
+
+/* Drop-in for AnACor/src/ray_tracing.c:484-534 (bound at
+ * utils_gridding.py:104-118): one voxel's map value for one direction
+ * (IsExp = 0: sum_m mu_m L_m; 1: exp(-sum)).  NaN with
+ * ANACOR_ERR_ASSERT where the reference asserts (angles not those of
+ * rotated_s1).  The volume is cached on the GPU by row-table address and shape
+ * between calls. */
+double ray_tracing_single_gridding(int64_t *coord, const double *rotated_s1, double theta, double phi,
+                                   double *voxel_size, double *coefficients, int8_t ***label_list, int64_t *shape,
+                                   int full_iteration, int index, int IsExp);
+/* Drop-in for AnACor/src/ray_tracing.c:427-482 (bound at
+ * utils_gridding.py:120-134): the bisection method is not implemented; NaN
+ * with ANACOR_ERR_UNSUPPORTED. */
+double ib_single_gridding(int64_t *coord, const double *rotated_s1, double theta, double phi, double *voxel_size,
+                          double *coefficients, int8_t ***label_list, int64_t *shape, int full_iteration, int index,
+                          int num_cls, int IsExp);
+/* Drop-in for AnACor/src/gridding_interpolation.c:100-163 (bound at
+ * utils_gridding.py:547-573): the padded map in the reference's layout
+ * [len_coord_list][ny][nx] (FP64), interpolation_method 1 nearest / 2
+ * bilinear.  Returns a malloc()ed array (free() it) or NULL with
+ * anacor_last_error(). */
+double *nearest_neighbor_interpolate_overall(int64_t low, int64_t up, int64_t *coord_list, int64_t len_coord_list,
+                                             const double *scattering_vector_list, const double *omega_list,
+                                             const double *raw_xray, const double *omega_axis,
+                                             const double *kp_rotation_matrix, int64_t len_result,
+                                             double *voxel_size, double *coefficients, int num_workers, int IsExp,
+                                             double *theta_list, double *phi_list, double *gridding_data, size_t nx,
+                                             size_t ny, double theta_min, double theta_max, double phi_min,
+                                             double phi_max, int interpolation_method);
+
 /* ------------------------------------------------------ learned surrogate -- */
 
 /* No counterpart in the reference (its absorption factors always come from

@@ -187,8 +187,27 @@ class Reference:
         lib.dials_2_thetaphi_22.argtypes = [_f64p, ct.c_int64]
         lib.dials_2_myframe.restype = None
         lib.dials_2_myframe.argtypes = [_f64p, _f64p]
+        lib.ray_tracing_single_gridding.restype = ct.c_double
+        lib.ray_tracing_single_gridding.argtypes = [_i64p, _f64p, ct.c_double, ct.c_double, _f64p, _f64p,
+                                                    ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8))), _i64p, ct.c_int,
+                                                    ct.c_int, ct.c_int]
         lib.free.argtypes = [ct.c_void_p]
         self.lib = lib
+
+    def single_gridding(self, coords, rotated_s1, theta, phi, voxel, mu, label, full_iteration=0, is_exp=0):
+        """ray_tracing_single_gridding (AnACor/src/ray_tracing.c:484-534) for
+        every voxel of `coords` and one direction: [n] doubles."""
+        label = _c(label, np.int8)
+        tab, keep = row_table(label)
+        shape = np.array(label.shape, dtype=np.int64)
+        out = np.empty(len(coords))
+        s = _c(rotated_s1, np.float64)
+        for k, c in enumerate(_c(coords, np.int64)):
+            out[k] = self.lib.ray_tracing_single_gridding(np.ascontiguousarray(c), s.copy(), float(theta),
+                                                          float(phi), _c(voxel, np.float64), _c(mu, np.float64),
+                                                          tab, shape, full_iteration, 0, is_exp)
+        del keep
+        return out
 
     def overall(self, s, num_workers: int = 1, full_iteration: int = 0) -> np.ndarray:
         label = _c(s.label, np.int8)

@@ -148,9 +148,9 @@ def trained_small(small):
     s = small
     omega, s1, ah = surrogate.training_set(s, n=16384, seed=21)
     x7 = surrogate.inputs(omega, s1, s.xray, s.omega_axis, s.F)
-    model = surrogate.Surrogate(members=4, seed=1, fourier_scale=1.0)
+    model = surrogate.Surrogate(members=4, seed=1, fourier_scale=0.5)
     model.set_data(x7, np.log(ah))
-    loss = model.train(1500, batch=2048, lr_max=2e-3, lr_min=2e-5, total_steps=1500)
+    loss = model.train(1500, batch=2048, lr_max=3e-3, lr_min=3e-5, total_steps=1500)
     yield model, loss
     model.close()
 

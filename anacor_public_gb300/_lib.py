@@ -41,6 +41,7 @@ EXPORTS = (
     "anacor_gridding_axes", "anacor_gridding_device_map", "anacor_gridding_map", "anacor_gridding_set_map",
     "anacor_gridding_interpolate", "anacor_gridding_interpolate_async", "anacor_gridding_destroy",
     "ray_tracing_single_gridding", "ib_single_gridding", "nearest_neighbor_interpolate_overall",
+    "anacor_plan_create_sampled", "anacor_plan_n_voxels", "anacor_plan_voxels", "anacor_sample_voxels",
 )
 
 _LIB = None
@@ -209,6 +210,15 @@ def load(path: str | None = None) -> ct.CDLL:
             np.ctypeslib.ndpointer(dtype=np.float64), _int, _int, np.ctypeslib.ndpointer(dtype=np.float64),
             np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64), ct.c_int64,
             ct.c_int64, ct.c_double, ct.c_double, ct.c_double, ct.c_double, _int]),
+    })
+    # GPU voxel sampling
+    sigs.update({
+        "anacor_plan_create_sampled": (_vp, [_i8p, _i64p, _int, _int, ct.c_int64, ct.c_double, _int, _f64p, _f64p,
+                                             _int, _int]),
+        "anacor_plan_n_voxels": (ct.c_int64, [_vp]),
+        "anacor_plan_voxels": (_int, [_vp, _i64p]),
+        "anacor_sample_voxels": (_int, [_i8p, _i64p, _int, _int, ct.c_int64, ct.c_double, _int, _vp, ct.c_int64,
+                                        ct.POINTER(ct.c_int64)]),
     })
     for name, (res, args) in sigs.items():
         getattr(L, name).restype = res

@@ -248,17 +248,14 @@ void plan_release(anacor_plan *p)
     cudaStreamSynchronize(st);
 }
 
-// `morton`: pack the voxel list in Morton order (A_h does not depend on the
-// order); per-voxel outputs keep the caller's order instead.
-int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
-              const double *voxel, const double *mu, int full, int is_exp, bool morton = true)
+// Volume, tables and sizes of a plan (the voxel list comes next).
+int plan_init_volume(anacor_plan *p, const int8_t *label, const int64_t *shape, const double *voxel, const double *mu,
+                     int full, int is_exp, bool morton)
 {
-    if (!label || !shape || !coords || !voxel || !mu)
+    if (!label || !shape || !voxel || !mu)
         return fail(kErrArgs, "null argument");
     if (!valid_shape(shape))
         return fail(kErrArgs, "volume axes must lie in [1, 8191] and the volume below 2^31 voxels");
-    if (n < 0 || n >= (1ll << 31))
-        return fail(kErrArgs, "coordinate count out of range");
     DeviceState *dev = nullptr;
     if (int st = current_device(&dev))
         return st;
@@ -270,29 +267,19 @@ int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const i
     }
     for (int a = 0; a < 4; a++)
         p->mu[a] = mu[a];
-    p->n_vox = (int)n;
     p->full = full;
     p->is_exp = is_exp;
     p->morton = morton;
     p->tile = kTile;
-    p->tiles = (int)((n + kTile - 1) / kTile);
     cudaStream_t st = p->stream;
     const size_t nvol = (size_t)shape[0] * shape[1] * shape[2];
     cudaError_t e;
-    if ((e = dev_alloc(&p->d_vol, nvol, st)) != cudaSuccess || (e = dev_alloc(&p->d_coords, (size_t)n, st)) ||
-        (e = dev_alloc(&p->d_status, 1, st)) || (e = dev_alloc(&p->d_counter, 1, st)) ||
-        (e = dev_alloc(&p->d_desc, 1, st)) || (e = dev_alloc(&p->d_c64, (size_t)n * 3, st)))
+    if ((e = dev_alloc(&p->d_vol, nvol, st)) != cudaSuccess || (e = dev_alloc(&p->d_status, 1, st)) ||
+        (e = dev_alloc(&p->d_counter, 1, st)) || (e = dev_alloc(&p->d_desc, 1, st)))
         return cuda_fail(e, "device allocation");
-    long long *d_c64 = p->d_c64;
     if ((e = cudaMemcpyAsync(p->d_vol, label, nvol, cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemsetAsync(p->d_status, 0, sizeof(int), st)))
         return cuda_fail(e, "volume upload");
-    if (n > 0) {
-        if ((e = cudaMemcpyAsync(d_c64, coords, (size_t)n * 3 * sizeof(long long), cudaMemcpyHostToDevice, st)) ||
-            (e = morton ? launch_pack_coords_morton(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)
-                        : launch_pack_coords(d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)))
-            return cuda_fail(e, "coordinate upload");
-    }
     // squared axis lengths for cal_path2_plus's total, as the reference
     // computes them: pow((last - first) * voxel, 2) == t * t, t = d * voxel
     p->sq_stride = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
@@ -307,6 +294,93 @@ int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const i
         (e = cudaStreamSynchronize(st)))
         return cuda_fail(e, "table upload");
     p->d_qtab = quotient_table(dev, p->sq_stride);
+    return kOk;
+}
+
+// The voxel list: the caller's int64 (z, y, x) rows, from host or device
+// memory, kept as given (d_c64) and packed for the kernels.
+int plan_set_voxels(anacor_plan *p, const int64_t *coords, int64_t n, bool on_device)
+{
+    if (n < 0 || n >= (1ll << 31))
+        return fail(kErrArgs, "coordinate count out of range");
+    if (n > 0 && !coords)
+        return fail(kErrArgs, "null argument");
+    cudaStream_t st = p->stream;
+    dev_free(p->d_coords, st);
+    dev_free(p->d_c64, st);
+    p->n_vox = (int)n;
+    p->tiles = (int)((n + p->tile - 1) / p->tile);
+    cudaError_t e;
+    if ((e = dev_alloc(&p->d_coords, (size_t)n, st)) || (e = dev_alloc(&p->d_c64, (size_t)n * 3, st)))
+        return cuda_fail(e, "device allocation");
+    if (n > 0) {
+        if ((e = cudaMemcpyAsync(p->d_c64, coords, (size_t)n * 3 * sizeof(long long),
+                                 on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st)) ||
+            (e = p->morton ? launch_pack_coords_morton(p->d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)
+                           : launch_pack_coords(p->d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)) ||
+            (e = cudaStreamSynchronize(st)))
+            return cuda_fail(e, "coordinate upload");
+    }
+    return kOk;
+}
+
+// `morton`: pack the voxel list in Morton order (A_h does not depend on the
+// order); per-voxel outputs keep the caller's order instead.
+int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
+              const double *voxel, const double *mu, int full, int is_exp, bool morton = true)
+{
+    if (!coords)
+        return fail(kErrArgs, "null argument");
+    if (n < 0 || n >= (1ll << 31))
+        return fail(kErrArgs, "coordinate count out of range");
+    if (int st = plan_init_volume(p, label, shape, voxel, mu, full, is_exp, morton))
+        return st;
+    return plan_set_voxels(p, coords, n, false);
+}
+
+// Crystal voxels of the plan's volume chosen on the device (method 0: all,
+// 1: the reference's 'even' picks, 2: stride lattice) into a fresh device
+// int64 [n][3] list (freed by the caller with cudaFreeAsync on the plan stream).
+int sample_voxels_device(anacor_plan *p, int code, int method, int64_t sampling_size, double sampling_ratio,
+                         int stride, long long **d_out, int64_t *n_out)
+{
+    cudaStream_t st = p->stream;
+    const int lattice = method == 2 ? stride : 1;
+    long long *d_count = nullptr, *d_lin = nullptr;
+    long long M = 0;
+    cudaError_t e;
+    if ((e = dev_alloc(&d_count, 1, st)) || (e = count_sampled_voxels(p->d_vol, p->dims, code, lattice, d_count, st)) ||
+        (e = cudaMemcpyAsync(&M, d_count, sizeof(long long), cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st))) {
+        dev_free(d_count, st);
+        return cuda_fail(e, "voxel count");
+    }
+    // the number kept (AnACor/utils/utils_rt.py:55-67)
+    long long n = M;
+    double step = 0.0;
+    if (method == 1) {
+        if (sampling_ratio > 0.0)
+            n = (long long)((double)M * sampling_ratio / 100.0);
+        else
+            n = M < sampling_size ? M : M / sampling_size;
+        step = n > 0 ? (double)M / (double)n : 0.0;
+        if (step == 0.0)
+            n = 0;
+    }
+    long long *d_c = nullptr;
+    if ((e = dev_alloc(&d_lin, (size_t)std::max(1ll, M), st)) ||
+        (e = select_sampled_voxels(p->d_vol, p->dims, code, lattice, d_lin, d_count, st)) ||
+        (e = dev_alloc(&d_c, (size_t)std::max(1ll, n) * 3, st)) ||
+        (e = unravel_voxels(d_lin, n, step, p->dims, d_c, st)) || (e = cudaStreamSynchronize(st))) {
+        dev_free(d_count, st);
+        dev_free(d_lin, st);
+        dev_free(d_c, st);
+        return cuda_fail(e, "voxel selection");
+    }
+    dev_free(d_count, st);
+    dev_free(d_lin, st);
+    *d_out = d_c;
+    *n_out = n;
     return kOk;
 }
 
@@ -654,6 +728,83 @@ anacor_plan *anacor_plan_create(const int8_t *label, const int64_t *shape, const
     }
     succeed();
     return p;
+}
+
+anacor_plan *anacor_plan_create_sampled(const int8_t *label, const int64_t *shape, int crystal_code, int method,
+                                        int64_t sampling_size, double sampling_ratio, int stride, const double *voxel,
+                                        const double *mu, int full_iteration, int is_exp)
+{
+    if (method < 0 || method > 2 || (method == 1 && sampling_size <= 0 && !(sampling_ratio > 0.0)) ||
+        (method == 2 && stride < 1)) {
+        fail(kErrArgs, "sampling: method 0 (all), 1 (even: sampling_size > 0 or ratio > 0) or 2 (stride >= 1)");
+        return nullptr;
+    }
+    anacor_plan *p = new (std::nothrow) anacor_plan();
+    if (!p) {
+        fail(kErrNoMem, "out of host memory");
+        return nullptr;
+    }
+    long long *d_c = nullptr;
+    int64_t n = 0;
+    int st = plan_init_volume(p, label, shape, voxel, mu, full_iteration, is_exp, true);
+    if (!st)
+        st = sample_voxels_device(p, crystal_code, method, sampling_size, sampling_ratio, stride, &d_c, &n);
+    if (!st)
+        st = plan_set_voxels(p, reinterpret_cast<const int64_t *>(d_c), n, true);
+    if (d_c)
+        dev_free(d_c, p->stream);
+    if (st) {
+        const int keep = t_status;
+        const std::string msg = t_msg;
+        if (p->stream)
+            plan_release(p);
+        delete p;
+        t_status = keep;
+        t_msg = msg;
+        return nullptr;
+    }
+    succeed();
+    return p;
+}
+
+int64_t anacor_plan_n_voxels(const anacor_plan *p) { return p ? p->n_vox : 0; }
+
+int anacor_plan_voxels(const anacor_plan *p, int64_t *coords_out)
+{
+    if (!p || !coords_out)
+        return fail(kErrArgs, "bad arguments");
+    cudaError_t e;
+    if (p->n_vox > 0 && ((e = cudaMemcpyAsync(coords_out, p->d_c64, (size_t)p->n_vox * 3 * sizeof(long long),
+                                              cudaMemcpyDeviceToHost, p->stream)) ||
+                         (e = cudaStreamSynchronize(p->stream))))
+        return cuda_fail(e, "voxel download");
+    return succeed();
+}
+
+int anacor_sample_voxels(const int8_t *label, const int64_t *shape, int crystal_code, int method,
+                         int64_t sampling_size, double sampling_ratio, int stride, int64_t *coords_out,
+                         int64_t capacity, int64_t *n_out)
+{
+    if (!n_out)
+        return fail(kErrArgs, "null argument");
+    const double vox[3] = {1.0, 1.0, 1.0}, mu[4] = {0.0, 0.0, 0.0, 0.0};
+    anacor_plan *p = anacor_plan_create_sampled(label, shape, crystal_code, method, sampling_size, sampling_ratio,
+                                                stride, vox, mu, 0, 1);
+    if (!p)
+        return t_status;
+    *n_out = p->n_vox;
+    int st = kOk;
+    if (p->n_vox > capacity || (p->n_vox > 0 && !coords_out))
+        st = fail(kErrArgs, "sampling: the output holds fewer rows than were selected (n_out has the count)");
+    else
+        st = anacor_plan_voxels(p, coords_out);
+    const int keep = t_status;
+    const std::string msg = t_msg;
+    plan_release(p);
+    delete p;
+    t_status = keep;
+    t_msg = msg;
+    return st;
 }
 
 int anacor_plan_set_reflections(anacor_plan *p, const double *s1, const double *omega, int64_t n_refl,

@@ -96,6 +96,16 @@ cudaError_t launch_pack_coords(const long long *d_c, int n, const int *dims, sho
 // Same, with the packed list sorted by the Morton code of (z, y, x).
 cudaError_t launch_pack_coords_morton(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
                                       cudaStream_t st);
+// Crystal-voxel sampling (sampling.cu): voxels with label == code (and, for
+// stride > 1, z, y, x multiples of stride) in C order as linear indices;
+// unravel_voxels writes (z, y, x) int64 of entry floor(j * step) (step > 0,
+// the reference's 'even' picks) or of every entry (step == 0).
+cudaError_t count_sampled_voxels(const int8_t *d_vol, const int *dims, int code, int stride, long long *d_count,
+                                 cudaStream_t st);
+cudaError_t select_sampled_voxels(const int8_t *d_vol, const int *dims, int code, int stride, long long *d_lin,
+                                  long long *d_count, cudaStream_t st);
+cudaError_t unravel_voxels(const long long *d_lin, long long n_out, double step, const int *dims, long long *d_coords,
+                           cudaStream_t st);
 // perm[k] = index in the caller's list of the k-th voxel of the Morton-packed list
 cudaError_t launch_morton_permutation(const long long *d_c, int n, const int *dims, int *d_perm, cudaStream_t st);
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs

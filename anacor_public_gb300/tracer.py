@@ -57,6 +57,35 @@ class Plan:
         self.n_refl = 0
 
     @classmethod
+    def from_volume(cls, label, voxel, mu, crystal_code: int = 3, method: str = "all", sampling_size: int = 5000,
+                    sampling_ratio: float | None = None, stride: int = 1, full_iteration=0, is_exp=1):
+        """A plan whose crystal-voxel list is chosen on the GPU from the volume
+        (uploaded once): method "all", "even" (the reference's default
+        sampling) or "stride" (z, y, x multiples of `stride`)."""
+        self = cls.__new__(cls)
+        self._L = _lib.load()
+        label = _c(label, np.int8)
+        self.shape = label.shape
+        m = {"all": 0, "even": 1, "stride": 2}[method]
+        h = self._L.anacor_plan_create_sampled(label, np.array(label.shape, dtype=np.int64), int(crystal_code), m,
+                                               int(sampling_size), float(sampling_ratio or 0.0), int(stride),
+                                               _c(voxel, np.float64), _c(mu, np.float64), int(full_iteration),
+                                               int(is_exp))
+        if not h:
+            st, msg = _lib.last_error(self._L)
+            raise _lib.AnacorError(st, msg)
+        self._h = ct.c_void_p(h)
+        self.n_vox = int(self._L.anacor_plan_n_voxels(self._h))
+        self.n_refl = 0
+        return self
+
+    def voxels(self) -> np.ndarray:
+        """The plan's voxel list [n][3] int64 (z, y, x)."""
+        out = np.zeros((max(self.n_vox, 1), 3), dtype=np.int64)
+        _lib.check(self._L.anacor_plan_voxels(self._h, out), self._L)
+        return out[:self.n_vox]
+
+    @classmethod
     def from_sample(cls, s, **kw):
         p = cls(s.label, s.coords, s.voxel, s.mu, **kw)
         p.set_reflections(s.s1, s.omega, s.xray, s.omega_axis, s.F)
@@ -178,6 +207,16 @@ def batch_run(plans, stream: int | None = None):
     L = _lib.load()
     arr = (ct.c_void_p * len(plans))(*[p._h.value for p in plans])
     _lib.check(L.anacor_batch_run(arr, len(plans), ct.c_void_p(stream or 0)), L)
+
+
+def sample_voxels(label, crystal_code: int = 3, method: str = "all", sampling_size: int = 5000,
+                  sampling_ratio: float | None = None, stride: int = 1) -> np.ndarray:
+    """Crystal-voxel list of a volume selected on the GPU (see Plan.from_volume)."""
+    p = Plan.from_volume(label, np.ones(3), np.zeros(4), crystal_code, method, sampling_size, sampling_ratio, stride)
+    try:
+        return p.voxels()
+    finally:
+        p.close()
 
 
 def rotated_vectors(omega_axis, omega, F, xray, s1):

@@ -194,6 +194,27 @@ int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *shape, const
                               const double *voxel, const double *mu, int full_iteration, int is_exp,
                               double *d_out, void *stream);
 
+/* ---------------------------------------------------- GPU voxel sampling -- */
+
+/* The crystal-voxel list chosen on the GPU from a volume uploaded once
+ * (AnACor/utils/utils_rt.py:27-253 samples on the host with np.where):
+ * method 0 every voxel with label == crystal_code, in C order; 1 the
+ * reference's 'even' method, entries np.linspace(0, M, n, endpoint=False,
+ * dtype=int) of that list with n = int(M * sampling_ratio / 100) when
+ * sampling_ratio > 0, else M // sampling_size (M when M < sampling_size); 2
+ * the stride lattice (z, y, x multiples of stride).  Rows are int64 (z, y, x). */
+anacor_plan *anacor_plan_create_sampled(const int8_t *label, const int64_t *shape, int crystal_code, int method,
+                                        int64_t sampling_size, double sampling_ratio, int stride, const double *voxel,
+                                        const double *mu, int full_iteration, int is_exp);
+int64_t anacor_plan_n_voxels(const anacor_plan *p);
+/* the plan's voxel list [n][3] in the order it was given or selected */
+int anacor_plan_voxels(const anacor_plan *p, int64_t *coords_out);
+/* the same selection returned to the host (capacity rows; *n_out = count,
+ * ANACOR_ERR_ARGS when capacity is too small) */
+int anacor_sample_voxels(const int8_t *label, const int64_t *shape, int crystal_code, int method,
+                         int64_t sampling_size, double sampling_ratio, int stride, int64_t *coords_out,
+                         int64_t capacity, int64_t *n_out);
+
 /* ------------------------------------------------ gridding (absorption map) -- */
 
 /* The reference's approximate mode (AnACor/utils/utils_gridding.py:63-473):

@@ -3,6 +3,9 @@
 ``python_2_c_3d``   int8*** row table over a C-contiguous volume
                     (AnACor/utils/utils_os.py:45-68), built in one pass.
 ``kp_rotation``     Rodrigues matrix (AnACor/utils/utils_os.py:26-43).
+``parse_reflections`` s1 vectors and rotation angles of reflection rows
+                    (AnACor/utils/utils_mp.py:151-164) in one pass instead of
+                    two ast.literal_eval calls per row.
 ``worker_function`` same arguments and outputs as the GPU/OpenMP branch of
                     AnACor/utils/utils_mp.py:39-212,418-432: parses ``s1`` and
                     the rotation angle of every selected reflection, calls
@@ -71,20 +74,40 @@ def ray_tracing_overall(label_list, coord_list, s1, omega, xray, omega_axis, F, 
     return out
 
 
+def _numbers(values, width: int) -> np.ndarray:
+    """Rows of `width` numbers from their JSON/Python literal strings (or
+    sequences) as float64.  Each number goes through float(), the conversion
+    ast.literal_eval applies to a numeric literal, so the values are identical."""
+    if not values:
+        return np.zeros((0, width))
+    if all(isinstance(v, str) for v in values):
+        text = ",".join(values).translate(_STRIP)
+        out = np.fromiter(map(float, text.split(",")), dtype=np.float64, count=len(values) * width)
+        return out.reshape(-1, width)
+    return np.array([literal_eval(v) if isinstance(v, str) else v for v in values], dtype=np.float64).reshape(
+        -1, width)
+
+
+_STRIP = str.maketrans("", "", "[]() \t\n")
+
+
+def parse_reflections(selected_data, offset: float = 0.0):
+    """(s1 [n][3], omega [n]) of reflection rows as the reference's worker
+    reads them: s1 = row["s1"], omega = row["xyzobs.mm.value"][2] + offset
+    (degrees) converted to radians (AnACor/utils/utils_mp.py:151-164)."""
+    s1 = _numbers([row["s1"] for row in selected_data], 3)
+    obs = _numbers([row["xyzobs.mm.value"] for row in selected_data], 3)
+    omega = obs[:, 2] + offset / 180 * np.pi
+    return s1, omega
+
+
 def worker_function(t1, low, dataset, selected_data, label_list, voxel_size, coefficients, F, coord_list,
                     omega_axis, axes_data, save_dir, args, offset, full_iteration, store_paths, printing,
                     num_cls, logger):
     """Same contract as AnACor/utils/utils_mp.py:39 for the --gpu / --openmp branch."""
     xray = -np.array(axes_data[1]["direction"])
     up = low + len(selected_data)
-    arr_scattering, arr_omega = [], []
-    for row in selected_data:
-        arr_scattering.append(literal_eval(row["s1"]) if isinstance(row["s1"], str) else row["s1"])
-        angle = literal_eval(row["xyzobs.mm.value"]) if isinstance(row["xyzobs.mm.value"], str) \
-            else row["xyzobs.mm.value"]
-        arr_omega.append(angle[2] + offset / 180 * np.pi)
-    arr_scattering = np.array(arr_scattering, dtype=np.float64).reshape(-1, 3)
-    arr_omega = np.array(arr_omega, dtype=np.float64)
+    arr_scattering, arr_omega = parse_reflections(selected_data, offset)
     if logger is not None:
         logger.info("GB300 absorption path is used for ray tracing")
     corr = list(ray_tracing_overall(label_list, coord_list, arr_scattering, arr_omega, xray, omega_axis, F,

@@ -42,6 +42,7 @@ EXPORTS = (
     "anacor_gridding_interpolate", "anacor_gridding_interpolate_async", "anacor_gridding_destroy",
     "ray_tracing_single_gridding", "ib_single_gridding", "nearest_neighbor_interpolate_overall",
     "anacor_plan_create_sampled", "anacor_plan_n_voxels", "anacor_plan_voxels", "anacor_sample_voxels",
+    "anacor_plan_run_bisection", "anacor_bisection",
 )
 
 _LIB = None
@@ -211,8 +212,11 @@ def load(path: str | None = None) -> ct.CDLL:
             np.ctypeslib.ndpointer(dtype=np.float64), np.ctypeslib.ndpointer(dtype=np.float64), ct.c_int64,
             ct.c_int64, ct.c_double, ct.c_double, ct.c_double, ct.c_double, _int]),
     })
-    # GPU voxel sampling
+    # GPU voxel sampling, bisection
     sigs.update({
+        "anacor_plan_run_bisection": (_int, [_vp, _int, _vp]),
+        "anacor_bisection": (_int, [_i8p, _i64p, _i64p, ct.c_int64, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p,
+                                    _f64p, _f64p, _int, _f64p]),
         "anacor_plan_create_sampled": (_vp, [_i8p, _i64p, _int, _int, ct.c_int64, ct.c_double, _int, _f64p, _f64p,
                                              _int, _int]),
         "anacor_plan_n_voxels": (ct.c_int64, [_vp]),

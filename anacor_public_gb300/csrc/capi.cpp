@@ -511,10 +511,26 @@ int plan_fetch(anacor_plan *p, double *out, cudaStream_t st)
 }
 
 // transient plan: upload, set up, run, fetch (the drop-in entry points)
+// the bisection variant (ib_test) over a plan's reflections
+int plan_launch_bisection(anacor_plan *p, cudaStream_t st, int num_cls)
+{
+    const long long items = (long long)p->n_refl * p->tiles;
+    if (items == 0)
+        return kOk;
+    static int bps = 0;
+    if (!bps && (bisection_occupancy(&bps) != kOk || bps <= 0))
+        bps = 1;
+    const int grid = (int)std::max(1ll, std::min(items, (long long)p->dev->sms * bps));
+    cudaError_t e = launch_bisection(p->d_desc, 1, items, p->d_counter, grid, num_cls, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "kernel launch");
+    return kOk;
+}
+
 int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, int64_t n, const double *voxel,
              const double *mu, int full, int is_exp, const double *s1, const double *omega, int64_t n_refl,
              const double *xray, const double *axis, const double *F, const ReflTable *tables, int threads,
-             double *out)
+             double *out, int ib_cls = 0)
 {
     anacor_plan p;
     int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
@@ -529,7 +545,7 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     if (!st)
         st = plan_upload_tables(&p);
     if (!st)
-        st = plan_launch(&p, p.stream);
+        st = ib_cls ? plan_launch_bisection(&p, p.stream, ib_cls) : plan_launch(&p, p.stream);
     if (!st)
         st = plan_fetch(&p, out, p.stream);
     const int keep = t_status;
@@ -833,6 +849,27 @@ int anacor_plan_run(anacor_plan *p, void *stream)
     return succeed();
 }
 
+int anacor_plan_run_bisection(anacor_plan *p, int num_cls, void *stream)
+{
+    if (!p || num_cls < 1)
+        return fail(kErrArgs, "bad arguments");
+    cudaStream_t st = stream ? (cudaStream_t)stream : p->stream;
+    if (int s = plan_launch_bisection(p, st, num_cls))
+        return s;
+    return succeed();
+}
+
+int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n_coords,
+                     const double *s1, const double *omega, int64_t n_refl, const double *xray,
+                     const double *omega_axis, const double *F, const double *voxel, const double *mu, int num_cls,
+                     double *out)
+{
+    if (n_refl < 0 || (n_refl > 0 && (!s1 || !omega || !xray || !omega_axis || !F || !out)) || num_cls < 1)
+        return fail(kErrArgs, "bad arguments");
+    return run_once(label, shape, coords, n_coords, voxel, mu, 0, 1, s1, omega, n_refl, xray, omega_axis, F,
+                    nullptr, 0, out, num_cls);
+}
+
 int anacor_plan_result(anacor_plan *p, double *out, void *stream)
 {
     if (!p || (!out && p->n_refl > 0))
@@ -1021,10 +1058,37 @@ double ib_test(int64_t *coord_list, int64_t len_coord_list, double *rotated_s1, 
                double *coefficients, int8_t ***label_list, int64_t *shape, int full_iteration, int64_t store_paths,
                int num_cls)
 {
-    (void)coord_list; (void)len_coord_list; (void)rotated_s1; (void)xray; (void)voxel_size;
-    (void)coefficients; (void)label_list; (void)shape; (void)full_iteration; (void)store_paths; (void)num_cls;
-    fail(kErrUnsupported, "ib_test: the iterative-bisection method is not provided by this library");
-    return std::nan("");
+    (void)full_iteration;
+    (void)store_paths;
+    const double nan = std::nan("");
+    if (!shape || !valid_shape(shape) || !rotated_s1 || !xray || !voxel_size || !coefficients || !coord_list ||
+        len_coord_list <= 0) {
+        fail(kErrArgs, "bad arguments");
+        return nan;
+    }
+    std::vector<int8_t> gathered;
+    const int8_t *flat = flat_base(label_list, shape);
+    if (!flat) {
+        if (!label_list) {
+            fail(kErrArgs, "null label table");
+            return nan;
+        }
+        gathered.resize((size_t)shape[0] * shape[1] * shape[2]);
+        for (int64_t z = 0; z < shape[0]; z++)
+            for (int64_t y = 0; y < shape[1]; y++)
+                std::memcpy(&gathered[(z * shape[1] + y) * shape[2]], label_list[z][y], (size_t)shape[2]);
+        flat = gathered.data();
+    }
+    ReflTable tab;
+    if (int st = setup_rotated(xray, rotated_s1, &tab)) {
+        fail(st, status_text(st));
+        return nan;
+    }
+    double out = nan;
+    if (run_once(flat, shape, coord_list, len_coord_list, voxel_size, coefficients, 0, 1, nullptr, nullptr, 1,
+                 nullptr, nullptr, nullptr, &tab, 0, &out, std::max(1, num_cls)))
+        return nan;
+    return out;
 }
 
 float *ray_tracing_gpu_overall(size_t low, size_t up, int *coord_list, size_t len_coord_list,

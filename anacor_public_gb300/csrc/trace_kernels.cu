@@ -585,6 +585,59 @@ __device__ __forceinline__ int find_sample(const SampleDesc *d, int n, long long
     return s;
 }
 
+// End of a work item: block reduction of the per-thread compensated sums
+// (warp-shuffle TwoSum, then across warps), the item's FP64 partial, and --
+// for the last tile of the reflection to arrive -- the fixed-order
+// combination of the partials into A_h.
+__device__ __forceinline__ void finish_item(float s, float c, const SampleDesc &D, long long r, int t, float *red_s,
+                                            float *red_c, int &last_s)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float so = __shfl_down_sync(kAll, s, o);
+        const float co = __shfl_down_sync(kAll, c, o);
+        float ns, e;
+        two_sum(s, so, ns, e);
+        s = ns;
+        c = c + co + e;
+    }
+    if (lane == 0) {
+        red_s[warp] = s;
+        red_c[warp] = c;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        float bs = red_s[0], bc = red_c[0];
+        for (int w = 1; w < kWarps; w++) {
+            float ns, e;
+            two_sum(bs, red_s[w], ns, e);
+            bs = ns;
+            bc = bc + red_c[w] + e;
+        }
+        D.partial[r * D.tiles + t] = (double)bs + (double)bc;
+        __threadfence();
+        const unsigned prev = atomicAdd(D.arrive + r, 1u);
+        last_s = prev == (unsigned)(D.tiles - 1);
+    }
+    __syncthreads();
+    if (last_s && warp == 0) {
+        // the last tile of this reflection combines all partials in a fixed order
+        __threadfence();
+        const volatile double *pp = D.partial + r * D.tiles;
+        double acc = 0.0;
+        for (int k = lane; k < D.tiles; k += 32)
+            acc += pp[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            acc += __shfl_down_sync(kAll, acc, o);
+        if (lane == 0) {
+            D.out[r] = acc / (double)D.n_vox;
+            D.arrive[r] = 0u;   // ready for the next launch
+        }
+    }
+}
+
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const SampleDesc *__restrict__ descs,
                                                                         int n_desc, long long total_items,
@@ -667,50 +720,198 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             if (lane == 0)
                 atomicAdd(D.steps, w);
         }
-        // warp-shuffle TwoSum reduction of (s, c)
+        finish_item(s, c, D, r, t, red_s, red_c, last_s);
+    }
+}
+
+// ---- iterative bisection (the reference's ib_test) ------------------------
+
+// One boundary search of AnACor/src/bisection.c:150-238 on the ray
+// c + m * q (q = the face rule's signed ratios, which are the ratios of the
+// reference's increments(), bisection.c:21-148): halve [shortest, longest]
+// down to the resolution 1.0; boundary 0: a label equal to cls moves longest
+// in, boundary 1: it moves shortest out.  The point is floor(c + floor(mid) q).
+// A position outside the volume (undefined in the reference) fails the ray.
+__device__ __forceinline__ bool bisect_dev(double longest, double shortest, int cz, int cy, int cx, const double *q,
+                                           const Vol &v, int boundary, int cls, int *p, double &mid)
+{
+    const double c[3] = {(double)cz, (double)cy, (double)cx};
+    const int dim[3] = {v.dz, v.dy, v.dx};
+    double diff = __dadd_rn(longest, -shortest);
+    mid = __dmul_rn(__dadd_rn(longest, shortest), 0.5);
+    while (diff > 1.0) {
+        mid = __dmul_rn(__dadd_rn(longest, shortest), 0.5);
+        int pp[3];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float so = __shfl_down_sync(kAll, s, o);
-            const float co = __shfl_down_sync(kAll, c, o);
+        for (int a = 0; a < 3; a++) {
+            const double x = floor(__dadd_rn(c[a], __dmul_rn(mid, q[a])));
+            if (!(x >= 0.0 && x < (double)dim[a]))
+                return false;
+            pp[a] = (int)x;
+        }
+        const int lab = __ldg(v.p + ((long long)pp[0] * v.dy + pp[1]) * v.dx + pp[2]);
+        const bool hit = lab == cls;
+        if (boundary == 0) {
+            if (hit) longest = mid; else shortest = mid;
+        } else {
+            if (hit) shortest = mid; else longest = mid;
+        }
+        diff = __dadd_rn(longest, -shortest);
+    }
+    const double fm = floor(mid);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        p[a] = (int)floor(__dadd_rn(c[a], __dmul_rn(fm, q[a])));
+    return true;
+}
+
+__device__ __forceinline__ double abs_sum3(const int *a, const int *b)
+{
+    return __dadd_rn(__dadd_rn(fabs((double)(a[0] - b[0])), fabs((double)(a[1] - b[1]))), fabs((double)(a[2] - b[2])));
+}
+
+// difference_length (bisection.c:260-270): z, then y, then x
+__device__ __forceinline__ double seg_len(const int *s, const int *e, const double *vox)
+{
+    const double dz = __dmul_rn((double)(s[0] - e[0]), vox[0]);
+    const double dy = __dmul_rn((double)(s[1] - e[1]), vox[1]);
+    const double dx = __dmul_rn((double)(s[2] - e[2]), vox[2]);
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dz, dz), __dmul_rn(dy, dy)), __dmul_rn(dx, dx)));
+}
+
+// iterative_bisection + cal_path_bisection (bisection.c:272-463) for one leg;
+// returns a status.  L = [liquor, loop, crystal, bubble].
+__device__ __noinline__ int ib_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx, const Vol &v,
+                                   int num_cls, const double *vox, double *L)
+{
+    L[0] = L[1] = L[2] = L[3] = 0.0;
+    const int face = exit_face(h, cz, cy, cx, v);
+    if (face == 0)
+        return kErrNoFace;
+    const FaceRule &R = rules[face - 1];
+    if (R.status)
+        return R.status;
+    double air_longest;
+    switch (face) {
+    case 4: air_longest = (double)cy; break;
+    case 5: air_longest = (double)(v.dy - 1 - cy); break;
+    case 6: air_longest = (double)cx; break;
+    case 1: air_longest = (double)(v.dx - 1 - cx); break;
+    case 2: air_longest = (double)cz; break;
+    default: air_longest = (double)(v.dz - 1 - cz); break;
+    }
+    const int p0[3] = {cz, cy, cx};
+    int air[3], cr[3], li[3], lo[3], bi[3], bo[3];
+    double m_air, m_cr, m_li, m_lo, m_bi, m_bo;
+    if (!bisect_dev(air_longest, 0.0, cz, cy, cx, R.q, v, 0, 0, air, m_air) ||
+        !bisect_dev(m_air, 0.0, cz, cy, cx, R.q, v, 1, 3, cr, m_cr))
+        return kErrArgs;
+    int npts = 3;
+    const int *pa = nullptr, *pb = nullptr, *pc = nullptr, *pd = nullptr;   // points 3..6
+    do {
+        if (!bisect_dev(m_air, m_cr, cz, cy, cx, R.q, v, 0, 2, li, m_li))
+            return kErrArgs;
+        if (__ddiv_rn(abs_sum3(li, air), 3.0) > 1.0) {
+            if (!bisect_dev(m_air, m_li, cz, cy, cx, R.q, v, 1, 2, lo, m_lo))
+                return kErrArgs;
+            if (__ddiv_rn(abs_sum3(li, lo), 3.0) <= 2.0)
+                break;
+            pa = li;
+            pb = lo;
+            npts = 5;
+        }
+        if (num_cls > 3) {
+            if (!bisect_dev(m_air, m_cr, cz, cy, cx, R.q, v, 0, 4, bi, m_bi))
+                return kErrArgs;
+            if (abs_sum3(bi, air) > 1.0) {
+                if (!bisect_dev(m_air, m_bi, cz, cy, cx, R.q, v, 1, 4, bo, m_bo))
+                    return kErrArgs;
+                if (__ddiv_rn(abs_sum3(bi, bo), 3.0) <= 2.0)
+                    break;
+                if (npts == 3) {
+                    pa = bi;
+                    pb = bo;
+                } else {
+                    pc = bi;
+                    pd = bo;
+                }
+                npts += 2;
+            }
+        }
+    } while (false);
+    const double total = seg_len(p0, air, vox);
+    const double cr_l = seg_len(p0, cr, vox);
+    double lo_l = 0.0, bu_l = 0.0;
+    // the lengths are read from the path by its length (5 points: loop, 7: bubble)
+    if (npts == 5)
+        lo_l = seg_len(pa, pb, vox);
+    else if (npts == 7)
+        bu_l = seg_len(pc, pd, vox);
+    L[0] = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(total, -lo_l), -bu_l), -cr_l), -0.0);
+    L[1] = lo_l;
+    L[2] = cr_l;
+    L[3] = bu_l;
+    return kOk;
+}
+
+// ib_test over every work item: as absorption_kernel, with bisection paths.
+__global__ void __launch_bounds__(kBlock, 2) bisection_kernel(const SampleDesc *__restrict__ descs, int n_desc,
+                                                              long long total_items,
+                                                              unsigned long long *__restrict__ work_counter,
+                                                              int num_cls)
+{
+    __shared__ ReflTable tab;
+    __shared__ float red_s[kWarps], red_c[kWarps];
+    __shared__ long long item_s;
+    __shared__ int last_s;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0)
+            item_s = (long long)atomicAdd(work_counter, 1ull);
+        __syncthreads();
+        const long long item = item_s;
+        if (item >= total_items)
+            break;
+        const int si = find_sample(descs, n_desc, item);
+        const SampleDesc &D = descs[si];
+        const long long local = item - D.work_begin;
+        const long long r = local / D.tiles;
+        const int t = (int)(local - r * D.tiles);
+        {
+            const int4 *src = reinterpret_cast<const int4 *>(D.refl + r);
+            int4 *dst = reinterpret_cast<int4 *>(&tab);
+            for (int k = tid; k < (int)(sizeof(ReflTable) / 16); k += kBlock)
+                dst[k] = __ldg(src + k);
+        }
+        __syncthreads();
+        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2]};
+        float s = 0.0f, c = 0.0f;
+        int bad = kOk;
+        const int v1 = min(D.n_vox, (t + 1) * D.tile);
+        for (int vi = t * D.tile + tid; vi < v1; vi += kBlock) {
+            const short4 cv = __ldg(D.coords + vi);
+            double a[4], b[4];
+            int st = ib_leg(tab.head[0], tab.rule[0], cv.x, cv.y, cv.z, v, num_cls, D.voxel, a);
+            if (!st)
+                st = ib_leg(tab.head[1], tab.rule[1], cv.x, cv.y, cv.z, v, num_cls, D.voxel, b);
+            if (st) {
+                bad |= st;
+                continue;
+            }
+            // cal_rate, operand order of AnACor/src/ray_tracing_basic.c:1573-1576
+            const double t0 = __dmul_rn(D.mu[0], __dadd_rn(a[0], b[0]));
+            const double t1 = __dmul_rn(D.mu[1], __dadd_rn(a[1], b[1]));
+            const double t2 = __dmul_rn(D.mu[2], __dadd_rn(a[2], b[2]));
+            const double t3 = __dmul_rn(D.mu[3], __dadd_rn(a[3], b[3]));
+            const double ex = __dadd_rn(__dadd_rn(__dadd_rn(t0, t1), t2), t3);
             float ns, e;
-            two_sum(s, so, ns, e);
+            two_sum(s, exp_neg(ex), ns, e);
             s = ns;
-            c = c + co + e;
+            c += e;
         }
-        if (lane == 0) {
-            red_s[warp] = s;
-            red_c[warp] = c;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            float bs = red_s[0], bc = red_c[0];
-            for (int w = 1; w < kWarps; w++) {
-                float ns, e;
-                two_sum(bs, red_s[w], ns, e);
-                bs = ns;
-                bc = bc + red_c[w] + e;
-            }
-            D.partial[r * D.tiles + t] = (double)bs + (double)bc;
-            __threadfence();
-            const unsigned prev = atomicAdd(D.arrive + r, 1u);
-            last_s = prev == (unsigned)(D.tiles - 1);
-        }
-        __syncthreads();
-        if (last_s && warp == 0) {
-            // the last tile of this reflection combines all partials in a fixed order
-            __threadfence();
-            const volatile double *pp = D.partial + r * D.tiles;
-            double acc = 0.0;
-            for (int k = lane; k < D.tiles; k += 32)
-                acc += pp[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1)
-                acc += __shfl_down_sync(kAll, acc, o);
-            if (lane == 0) {
-                D.out[r] = acc / (double)D.n_vox;
-                D.arrive[r] = 0u;   // ready for the next launch
-            }
-        }
+        if (bad)
+            atomicOr(D.status, 1 << bad);
+        finish_item(s, c, D, r, t, red_s, red_c, last_s);
     }
 }
 
@@ -932,6 +1133,25 @@ cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const
                                                                     d_coords, n, d_voxel, full, d_sq, sq_stride,
                                                                     d_qtab, face, len, nseg, first, last, L, status);
     return cudaGetLastError();
+}
+
+cudaError_t launch_bisection(const SampleDesc *d_descs, int n_desc, long long total_items,
+                             unsigned long long *d_counter, int grid, int num_cls, cudaStream_t st)
+{
+    if (total_items <= 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess)
+        return e;
+    bisection_kernel<<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter, num_cls);
+    return cudaGetLastError();
+}
+
+int bisection_occupancy(int *blocks_per_sm)
+{
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, bisection_kernel, kBlock, 0) == cudaSuccess
+               ? kOk
+               : kErrCuda;
 }
 
 cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,

@@ -116,6 +116,11 @@ cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const
                               int n, const double *d_voxel, int full, const double *d_sq, int sq_stride,
                               const double *d_qtab, int *face, int *len, int *nseg, int *first, int *last, double *L,
                               int *status, cudaStream_t st);
+// The reference's iterative-bisection variant (ib_test) over the same work
+// items as launch_absorption; num_cls > 3 also searches bubble boundaries.
+cudaError_t launch_bisection(const SampleDesc *d_descs, int n_desc, long long total_items,
+                             unsigned long long *d_counter, int grid, int num_cls, cudaStream_t st);
+int bisection_occupancy(int *blocks_per_sm);
 // Persistent launch over n_dirs * tiles work items of the map.
 cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,
                                 cudaStream_t st);

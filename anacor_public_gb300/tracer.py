@@ -35,6 +35,21 @@ def absorption(label, coords, s1, omega, xray, omega_axis, F, voxel, mu, full_it
     return out[:n]
 
 
+def bisection(label, coords, s1, omega, xray, omega_axis, F, voxel, mu, num_cls=4):
+    """A_h of every reflection with bisection paths (the reference's ib_test)."""
+    L = _lib.load()
+    label = _c(label, np.int8)
+    s1 = _c(s1, np.float64).reshape(-1, 3)
+    n = s1.shape[0]
+    out = np.zeros(max(n, 1), dtype=np.float64)
+    st = L.anacor_bisection(label, np.array(label.shape, dtype=np.int64), _c(coords, np.int64).reshape(-1, 3),
+                            len(coords), s1, _c(omega, np.float64), n, _c(xray, np.float64),
+                            _c(omega_axis, np.float64), _c(F, np.float64).reshape(-1), _c(voxel, np.float64),
+                            _c(mu, np.float64), int(num_cls), out)
+    _lib.check(st, L)
+    return out[:n]
+
+
 def sample_absorption(s, **kw):
     return absorption(s.label, s.coords, s.s1, s.omega, s.xray, s.omega_axis, s.F, s.voxel, s.mu, **kw)
 
@@ -102,6 +117,10 @@ class Plan:
     def run(self, stream: int | None = None):
         """Enqueue the march on `stream` (a raw cudaStream_t handle) or the plan's own stream."""
         _lib.check(self._L.anacor_plan_run(self._h, ct.c_void_p(stream or 0)), self._L)
+
+    def run_bisection(self, num_cls: int = 4, stream: int | None = None):
+        """Enqueue the bisection variant (the reference's ib_test per reflection)."""
+        _lib.check(self._L.anacor_plan_run_bisection(self._h, int(num_cls), ct.c_void_p(stream or 0)), self._L)
 
     def result(self, stream: int | None = None) -> np.ndarray:
         out = np.zeros(max(self.n_refl, 1), dtype=np.float64)

@@ -49,10 +49,13 @@ double ray_tracing_single(int64_t *coord_list, int64_t len_coord_list, const dou
                           const double *xray, double *voxel_size, double *coefficients, int8_t ***label_list,
                           int64_t *shape, int full_iteration, int64_t store_paths, int IsExp);
 
-/* Symbol of AnACor/src/ray_tracing.c:25-31 (ib_test, the iterative-bisection
- * variant).  AnACor's worker binds it at load time (utils_mp.py:95-109), so
- * it is exported; the bisection method is not part of this library and the
- * call returns NaN with status ANACOR_ERR_UNSUPPORTED. */
+/* Replaces AnACor/src/ray_tracing.c:25-163 (ib_test, the iterative-bisection
+ * variant, bound at utils_mp.py:95-109): A_h of one reflection from rotated
+ * vectors with each leg's class boundaries found by bisection
+ * (AnACor/src/bisection.c) instead of a march; num_cls > 3 also searches
+ * bubbles.  An approximation of ray_tracing_single.  NaN on error (the
+ * reference reads outside the volume where a search leaves it; here that is
+ * ANACOR_ERR_ARGS). */
 double ib_test(int64_t *coord_list, int64_t len_coord_list, double *rotated_s1, double *xray,
                double *voxel_size, double *coefficients, int8_t ***label_list, int64_t *shape,
                int full_iteration, int64_t store_paths, int num_cls);
@@ -127,6 +130,14 @@ int anacor_plan_count_steps(anacor_plan *p, uint64_t *total);
 /* Number of CTAs one run launches and the number of kernels it enqueues. */
 int anacor_plan_launch_info(const anacor_plan *p, int *grid, int *kernels);
 void anacor_plan_destroy(anacor_plan *p);
+/* The bisection variant (ib_test per reflection) over the plan's reflections;
+ * results as for anacor_plan_run. */
+int anacor_plan_run_bisection(anacor_plan *p, int num_cls, void *stream);
+/* ib_test for every reflection (omega, s1 as for anacor_absorption). */
+int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n_coords,
+                     const double *s1, const double *omega, int64_t n_refl, const double *xray,
+                     const double *omega_axis, const double *F, const double *voxel, const double *mu, int num_cls,
+                     double *out);
 
 /* Execution parameters of a plan (no counterpart in the reference; they do
  * not change the per-ray results, only the FP32 summation order of A_h):

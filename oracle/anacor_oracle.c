@@ -585,3 +585,172 @@ void oracle_reflection_dirs(const double *s1_rot, const double *xray_rot, double
         out10[7 + a] = d.d_out[a];
     }
 }
+
+/* ------------------------------------------------- iterative bisection */
+
+/* The reference's boundary search (AnACor/src/bisection.c:150-238): on the
+ * ray c + m * q (q as in face_rule, which equals the ratios of increments(),
+ * bisection.c:21-148, with the y sign folded), halve [shortest, longest] until
+ * it is at most `resolution` long.  boundary 0: a label equal to cls moves
+ * longest in; boundary 1: it moves shortest out.  The point returned is
+ * floor(c + floor(mid) * q).  Positions outside the volume are undefined in
+ * the reference; here they end the search with ORC_ERR_ARGS. */
+typedef struct {
+    int64_t p[3];
+    double mid;
+} orc_bis;
+
+static int bisect(double longest, double shortest, double resolution, const int64_t *c, const double *q,
+                  const int8_t *vol, const int64_t *shape, int boundary, int cls, orc_bis *out)
+{
+    double diff = longest - shortest;
+    double mid = (longest + shortest) / 2.0;
+    while (diff > resolution) {
+        mid = (longest + shortest) / 2.0;
+        int64_t p[3];
+        for (int a = 0; a < 3; a++) {
+            p[a] = (int64_t)floor((double)c[a] + mid * q[a]);
+            if (p[a] < 0 || p[a] >= shape[a])
+                return ORC_ERR_ARGS;
+        }
+        const int lab = vol[(p[0] * shape[1] + p[1]) * shape[2] + p[2]];
+        if (boundary == 0) {
+            if (lab == cls)
+                longest = mid;
+            else
+                shortest = mid;
+        } else {
+            if (lab == cls)
+                shortest = mid;
+            else
+                longest = mid;
+        }
+        diff = longest - shortest;
+    }
+    for (int a = 0; a < 3; a++)
+        out->p[a] = (int64_t)floor((double)c[a] + floor(mid) * q[a]);
+    out->mid = mid;
+    return ORC_OK;
+}
+
+/* difference_length (bisection.c:260-270): z, then y, then x */
+static double seg_len(const int64_t *s, const int64_t *e, const double *voxel)
+{
+    const double dz = (double)(s[0] - e[0]) * voxel[0];
+    const double dy = (double)(s[1] - e[1]) * voxel[1];
+    const double dx = (double)(s[2] - e[2]) * voxel[2];
+    return sqrt(dz * dz + dy * dy + dx * dx);
+}
+
+static double abs_sum3(const int64_t *a, const int64_t *b)
+{
+    return fabs((double)(a[0] - b[0])) + fabs((double)(a[1] - b[1])) + fabs((double)(a[2] - b[2]));
+}
+
+/* iterative_bisection (bisection.c:312-463) + cal_path_bisection (:272-310)
+ * for one leg: L = [liquor, loop, crystal, bubble].  The path holds the start
+ * voxel, the sample's outer boundary, the crystal's outer boundary, then a
+ * loop pair and a bubble pair when found; the lengths are read from the path
+ * by its length only (5 points: the pair is counted as loop, 7: only the
+ * second pair, as bubble), as the reference does. */
+static int ib_leg(const int64_t *c, int64_t face, double th, double ph, const int8_t *vol, const int64_t *shape,
+                  int num_cls, const double *voxel, double *L)
+{
+    orc_rule r;
+    int st = face_rule(face, th, ph, &r);
+    if (st)
+        return st;
+    const double res = 1.0;
+    double air_longest;
+    switch (face) {
+    case 4: air_longest = (double)c[1]; break;
+    case 5: air_longest = (double)(shape[1] - 1 - c[1]); break;
+    case 6: air_longest = (double)c[2]; break;
+    case 1: air_longest = (double)(shape[2] - 1 - c[2]); break;
+    case 2: air_longest = (double)c[0]; break;
+    default: air_longest = (double)(shape[0] - 1 - c[0]); break;
+    }
+    int64_t pts[7][3];
+    int n = 0;
+    for (int a = 0; a < 3; a++)
+        pts[0][a] = c[a];
+    n = 1;
+    orc_bis air, cr, li, lo, bi, bo;
+    if ((st = bisect(air_longest, 0.0, res, c, r.q, vol, shape, 0, 0, &air)))
+        return st;
+    memcpy(pts[n++], air.p, sizeof(air.p));
+    if ((st = bisect(air.mid, 0.0, res, c, r.q, vol, shape, 1, 3, &cr)))
+        return st;
+    memcpy(pts[n++], cr.p, sizeof(cr.p));
+    for (;;) {
+        if ((st = bisect(air.mid, cr.mid, res, c, r.q, vol, shape, 0, 2, &li)))
+            return st;
+        if (abs_sum3(li.p, air.p) / 3 > 1) {
+            if ((st = bisect(air.mid, li.mid, res, c, r.q, vol, shape, 1, 2, &lo)))
+                return st;
+            if (abs_sum3(li.p, lo.p) / 3 <= 2)
+                break;
+            memcpy(pts[n++], li.p, sizeof(li.p));
+            memcpy(pts[n++], lo.p, sizeof(lo.p));
+        }
+        if (num_cls > 3) {
+            if ((st = bisect(air.mid, cr.mid, res, c, r.q, vol, shape, 0, 4, &bi)))
+                return st;
+            if (abs_sum3(bi.p, air.p) > 1) {
+                if ((st = bisect(air.mid, bi.mid, res, c, r.q, vol, shape, 1, 4, &bo)))
+                    return st;
+                if (abs_sum3(bi.p, bo.p) / 3 <= 2)
+                    break;
+                memcpy(pts[n++], bi.p, sizeof(bi.p));
+                memcpy(pts[n++], bo.p, sizeof(bo.p));
+            }
+        }
+        break;
+    }
+    const double total = seg_len(pts[0], pts[1], voxel);
+    const double cr_l = seg_len(pts[0], pts[2], voxel);
+    double lo_l = 0, bu_l = 0;
+    if (n == 5)
+        lo_l = seg_len(pts[3], pts[4], voxel);
+    else if (n == 7)
+        bu_l = seg_len(pts[5], pts[6], voxel);
+    L[0] = total - lo_l - bu_l - cr_l - 0.0;
+    L[1] = lo_l;
+    L[2] = cr_l;
+    L[3] = bu_l;
+    return ORC_OK;
+}
+
+/* ib_test (AnACor/src/ray_tracing.c:25-163): mean over voxels of
+ * exp(-sum mu (L_incident + L_diffracted)) with bisection paths
+ * (resolution 1.0).  L_out (optional) receives [n][2][4] lengths. */
+int oracle_ib(const int64_t *coords, int64_t n, const double *s1_rot, const double *xray_rot, const double *voxel,
+              const double *mu, const int8_t *vol, const int64_t *shape, int num_cls, double *out, double *L_out)
+{
+    if (n <= 0 || check_coords(coords, n, shape))
+        return ORC_ERR_ARGS;
+    orc_dirs d;
+    reflection_dirs(s1_rot, xray_rot, &d);
+    double sum = 0;
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t *c = coords + 3 * k;
+        const int64_t f1 = oracle_cube_face(c, d.d_in, shape, 1);
+        const int64_t f2 = oracle_cube_face(c, d.d_out, shape, 0);
+        if (!f1 || !f2)
+            return ORC_ERR_FACE;
+        double l1[4], l2[4];
+        int st = ib_leg(c, f1, d.th_in, d.ph_in, vol, shape, num_cls, voxel, l1);
+        if (!st)
+            st = ib_leg(c, f2, d.th_out, d.ph_out, vol, shape, num_cls, voxel, l2);
+        if (st)
+            return st;
+        if (L_out)
+            for (int m = 0; m < 4; m++) {
+                L_out[8 * k + m] = l1[m];
+                L_out[8 * k + 4 + m] = l2[m];
+            }
+        sum += rate(l1, l2, mu, 1);
+    }
+    *out = sum / n;
+    return ORC_OK;
+}

@@ -59,6 +59,9 @@ class Oracle:
         lib.oracle_rotate.argtypes = [_f64p, ct.c_double, _f64p, _f64p, _f64p, _f64p, _f64p]
         lib.oracle_reflection_dirs.restype = None
         lib.oracle_reflection_dirs.argtypes = [_f64p, _f64p, _f64p]
+        lib.oracle_ib.restype = ct.c_int
+        lib.oracle_ib.argtypes = [_i64p, ct.c_int64, _f64p, _f64p, _f64p, _f64p, _i8p, _i64p, ct.c_int, _f64p,
+                                  ct.c_void_p]
         lib.oracle_cube_face.restype = ct.c_int64
         lib.oracle_cube_face.argtypes = [_i64p, _f64p, _i64p, ct.c_int]
         self.lib = lib
@@ -95,6 +98,20 @@ class Oracle:
         if st:
             raise RuntimeError(f"oracle_single: {STATUS.get(st, st)}")
         return float(out[0])
+
+    def ib(self, coords, s1_rot, xray_rot, voxel, mu, label, num_cls=4, lengths=False):
+        """ib_test's A_h (bisection paths) of one reflection; with lengths, also
+        the per-voxel [n][2][4] lengths.  Raises on a status."""
+        n = len(coords)
+        out = np.zeros(1)
+        L = np.zeros((n, 2, 4)) if lengths else None
+        st = self.lib.oracle_ib(_c(coords, np.int64), n, _c(s1_rot, np.float64), _c(xray_rot, np.float64),
+                                _c(voxel, np.float64), _c(mu, np.float64), _c(label, np.int8),
+                                np.array(label.shape, dtype=np.int64), int(num_cls), out,
+                                L.ctypes.data if L is not None else None)
+        if st:
+            raise RuntimeError(f"oracle_ib: {STATUS.get(st, st)}")
+        return (float(out[0]), L) if lengths else float(out[0])
 
     def leg_detail(self, coords, s1_rot, xray_rot, voxel, label, full_iteration=0) -> dict:
         n = len(coords)
@@ -191,8 +208,23 @@ class Reference:
         lib.ray_tracing_single_gridding.argtypes = [_i64p, _f64p, ct.c_double, ct.c_double, _f64p, _f64p,
                                                     ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8))), _i64p, ct.c_int,
                                                     ct.c_int, ct.c_int]
+        lib.ib_test.restype = ct.c_double
+        lib.ib_test.argtypes = [_i64p, ct.c_int64, _f64p, _f64p, _f64p, _f64p,
+                                ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8))), _i64p, ct.c_int, ct.c_int64,
+                                ct.c_int]
         lib.free.argtypes = [ct.c_void_p]
         self.lib = lib
+
+    def ib_test(self, coords, s1_rot, xray_rot, voxel, mu, label, num_cls=4) -> float:
+        """ib_test (AnACor/src/ray_tracing.c:25-163), bisection paths."""
+        label = _c(label, np.int8)
+        tab, keep = row_table(label)
+        with silence_stdout():
+            r = self.lib.ib_test(_c(coords, np.int64), len(coords), _c(s1_rot, np.float64).copy(),
+                                 _c(xray_rot, np.float64).copy(), _c(voxel, np.float64), _c(mu, np.float64), tab,
+                                 np.array(label.shape, dtype=np.int64), 0, 0, int(num_cls))
+        del keep
+        return float(r)
 
     def single_gridding(self, coords, rotated_s1, theta, phi, voxel, mu, label, full_iteration=0, is_exp=0):
         """ray_tracing_single_gridding (AnACor/src/ray_tracing.c:484-534) for

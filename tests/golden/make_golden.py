@@ -14,6 +14,11 @@ Fixtures (all small):
                     reference's cube_face / cal_coord / cal_path2_plus for a
                     voxel subset of 8 reflections.
   beamline_ah.npz   A_h of 12 reflections of the 512x512x400 stride-4 sample.
+  small_ib.npz      A_h of 30 reflections of the 96^3 sample from the
+                    reference's ib_test (iterative bisection), num_cls 4 and 3.
+  small_grid.npz    ray_tracing_single_gridding values (the gridding map) of
+                    64 voxels for 8 grid directions of a 36 x 18 grid, with the
+                    direction vectors built as the reference's gridding does.
   sphere_kat.npz    A_h of a voxelised sphere at mu*r = 0.1, 0.5, 1 and
                     2theta = linspace(0, 180, 10), from the reference's
                     ray_tracing_single, beside the analytic transmission values
@@ -84,9 +89,41 @@ def sphere_directions(two_theta_deg):
     return out
 
 
+def bisection_and_gridding(ref):
+    """Fixtures of the bisection and gridding modes (python make_golden.py --modes)."""
+    from oracle import gridding_oracle as go
+    s = synth.small_sample()
+    o = orc.Oracle()
+    refl = np.arange(0, s.n_refl, 10)
+    ib = {}
+    for ncls in (4, 3):
+        vals = []
+        for i in refl:
+            xr, sr = o.rotate(s, int(i))
+            vals.append(ref.ib_test(s.coords, sr, xr, s.voxel, s.mu, s.label, ncls))
+        ib[ncls] = vals
+    np.savez_compressed(os.path.join(HERE, "small_ib.npz"), refl=refl, ib4=np.array(ib[4]), ib3=np.array(ib[3]),
+                        digest=sample_digest(s))
+    s1, th, ph = go.directions(36, 18)
+    rng = np.random.default_rng(0)
+    dirs = np.sort(rng.choice(len(s1), 8, replace=False))
+    vox = np.ascontiguousarray(s.coords[np.sort(rng.choice(len(s.coords), 64, replace=False))])
+    vals, angles = [], []
+    for d in dirs:
+        tp = ref.lib.dials_2_thetaphi_22(np.ascontiguousarray(s1[d]).copy(), 0)
+        angles.append((tp.theta, tp.phi))
+        vals.append(ref.single_gridding(vox, s1[d], tp.theta, tp.phi, s.voxel, s.mu, s.label))
+    np.savez_compressed(os.path.join(HERE, "small_grid.npz"), dirs=dirs, s1=s1[dirs], angles=np.array(angles),
+                        coords=vox, value=np.array(vals))
+    print("ib", ib[4][:3], "grid", vals[0][:3])
+
+
 def main():
     orc.build_oracle(ref=True)
     ref = orc.Reference()
+    if "--modes" in sys.argv:
+        bisection_and_gridding(ref)
+        return
 
     s = synth.small_sample()
     ah = ref.overall(s, num_workers=os.cpu_count() or 1)
@@ -124,6 +161,7 @@ def main():
     for m in (0.1, 0.5, 1.0):
         err = np.abs(np.array(res[m]) - SPHERE_ANALYTIC[m]) / np.array(SPHERE_ANALYTIC[m])
         print("sphere mu*r", m, "max rel err vs analytic", err.max())
+    bisection_and_gridding(ref)
 
 
 if __name__ == "__main__":

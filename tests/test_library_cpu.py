@@ -51,12 +51,12 @@ def test_host_rotation_matches_oracle_bitwise(lib, oracle):
         assert np.array_equal(rx[i], xr) and np.array_equal(rs[i], sr)
 
 
-def test_ib_test_is_unsupported(lib):
+def test_ib_test_rejects_a_missing_table(lib):
     s = synth.small_sample(n_refl=1)
     r = lib.ib_test(s.coords, len(s.coords), s.s1[0].copy(), s.xray.copy(), s.voxel, s.mu, None,
                     s.shape, 0, 0, 4)
     assert np.isnan(r)
-    assert lib.anacor_last_status() == 6
+    assert lib.anacor_last_status() == 3
 
 
 def _no_gpu():

@@ -50,9 +50,13 @@ WORKLOADS = {
                  "re-traced by the plain kernel",
     "highabs_surrogate": "1024x1024x800 high-absorption sample, all crystal voxels; ensemble trained as for "
                          "the beamline sample; 50000 reflections with the 2% audit + spread fallback",
+    "gridding": "beamline sample; absorption map 360 x 180 directions x 22917 voxels built on the GPU, then "
+                "nearest-grid-point interpolation of 20000 reflections",
+    "bisection": "1024x1024x800 high-absorption sample, all crystal voxels; iterative-bisection paths "
+                 "(ib_test) on a reflection subset, beside the plain march",
 }
 DEFAULT_REFL = {"beamline": 20000, "small": 300, "batch": 0, "highabs": 256, "surrogate": 1000000,
-                "highabs_surrogate": 50000}
+                "highabs_surrogate": 50000, "gridding": 20000, "bisection": 256}
 SURROGATE_METRIC = "reflections/s (surrogate with audit: ensemble A_h, 2% random + high-spread re-traced)"
 
 
@@ -72,8 +76,8 @@ def parse():
     ap.add_argument("--train-steps", type=int, default=20000, help="surrogate: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096)
     ap.add_argument("--members", type=int, default=4)
-    ap.add_argument("--fourier-scale", type=float, default=1.0)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--fourier-scale", type=float, default=0.5)
+    ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--audit", type=float, default=0.02)
     ap.add_argument("--spread", type=float, default=1e-3)
     a = ap.parse_args()
@@ -99,6 +103,10 @@ def make_samples(args, rank: int = 0):
         ss = [synth.beamline_sample()]
     elif w == "highabs_surrogate":
         ss = [synth.high_absorption_sample(n_refl=256)]
+    elif w == "gridding":
+        ss = [synth.beamline_sample(n_refl=args.refl)]
+    elif w == "bisection":
+        ss = [synth.high_absorption_sample(n_refl=args.refl)]
     else:
         ss = synth.batch_samples(n_samples=12)
     if rank > 0:
@@ -647,12 +655,109 @@ def run_surrogate(args):
         torch.distributed.destroy_process_group()
 
 
+def _events_ms(torch, stream, fn, reps: int, flush=None):
+    ms = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    return ms
+
+
+def run_modes(args):
+    """The gridding and bisection rows: their own throughput on the device,
+    beside the plain march on the same sample, and their error against it."""
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    from anacor_public_gb300 import build, gridding, tracer
+    build.build()
+    s = make_samples(args, rank)[0]
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sh = stream.cuda_stream
+    plan = tracer.Plan.from_sample(s)
+    if not args.no_autotune:
+        plan.autotune()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    n, n_vox = s.n_refl, len(s.coords)
+    # the plain march on the same reflections (reference point and error baseline)
+    for _ in range(args.warmup):
+        plan.run(sh)
+    plain_ms = statistics.median(_events_ms(torch, stream, lambda: plan.run(sh), args.steps, flush))
+    plain = plan.result(sh)
+    extra = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if args.workload == "gridding":
+        g = gridding.GriddingMap(plan, 360, 180)
+        t0 = time.perf_counter()
+        g.build()
+        build_s = time.perf_counter() - t0
+        d_out = torch.empty(n, dtype=torch.float64, device="cuda")
+        run = lambda: g.interpolate_async(s.s1, s.omega, s.xray, s.omega_axis, s.F, d_out.data_ptr(), sh)  # noqa
+        for _ in range(args.warmup):
+            run()
+        ms = _events_ms(torch, stream, run, args.steps, flush)
+        approx = d_out.cpu().numpy()
+        map_rays = g.n_dirs * n_vox
+        extra = {"map_build_s": build_s, "map_directions": g.n_dirs, "map_rays_per_s": map_rays / build_s,
+                 "map_bytes": int(g.n_dirs * g.device_map()[1] * 4)}
+        alg_bytes = n * n_vox * 2 * 4
+        g.close()
+        kernels = 1
+    else:
+        run = lambda: plan.run_bisection(4, sh)  # noqa: E731
+        for _ in range(args.warmup):
+            run()
+        ms = _events_ms(torch, stream, run, args.steps, flush)
+        approx = plan.result(sh)
+        alg_bytes = None
+        kernels = 1
+    clk = clocks.stop()
+    ms_step = statistics.median(ms)
+    value = n / (ms_step / 1e3)
+    err = np.abs(approx - plain) / plain
+    if rank == 0:
+        peak, src = measured_peak_gbs()
+        achieved = alg_bytes / (ms_step / 1e3) / 1e9 if alg_bytes else None
+        line = {
+            "metric": f"reflections/s ({args.workload} mode, A_h per reflection)", "value": value,
+            "unit": "reflections/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload], "n_voxels": n_vox, "n_reflections": n,
+                       "volume": list(s.label.shape), "l2": "flushed between steps (256 MiB write)"},
+            "plain_refl_per_s": n / (plain_ms / 1e3), "speedup_vs_plain": plain_ms / ms_step,
+            "rel_err_vs_plain": _quantiles(err),
+            **extra,
+            "roofline": ({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                          "peak_source": src, "traffic": None,
+                          "alg_bytes_per_launch": alg_bytes, "kernel": "gridding_interp_kernel"}
+                         if achieved else None),
+            "cpu_baseline": None,
+            "e2e": None,
+            "clocks": clk,
+            "gpu_launches": args.steps * kernels,
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload in ("surrogate", "highabs_surrogate"):
         run_surrogate(args)
+    elif args.workload in ("gridding", "bisection"):
+        run_modes(args)
     else:
         run_ours(args)
 

@@ -42,7 +42,7 @@ EXPORTS = (
     "anacor_gridding_interpolate", "anacor_gridding_interpolate_async", "anacor_gridding_destroy",
     "ray_tracing_single_gridding", "ib_single_gridding", "nearest_neighbor_interpolate_overall",
     "anacor_plan_create_sampled", "anacor_plan_n_voxels", "anacor_plan_voxels", "anacor_sample_voxels",
-    "anacor_plan_run_bisection", "anacor_bisection",
+    "anacor_plan_run_bisection", "anacor_bisection", "anacor_gridding_prepare", "anacor_gridding_run",
 )
 
 _LIB = None
@@ -192,6 +192,8 @@ def load(path: str | None = None) -> ct.CDLL:
         "anacor_gridding_interpolate_async": (_int, [_vp, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p, _int,
                                                      _vp, _vp]),
         "anacor_gridding_destroy": (None, [_vp]),
+        "anacor_gridding_prepare": (_int, [_vp, _f64p, _f64p, ct.c_int64, _f64p, _f64p, _f64p, _int]),
+        "anacor_gridding_run": (_int, [_vp, _vp, _vp]),
         # drop-ins, argtypes as AnACor/utils/utils_gridding.py:104-134 and :547-573
         "ray_tracing_single_gridding": (ct.c_double, [np.ctypeslib.ndpointer(dtype=np.int64),
                                                       np.ctypeslib.ndpointer(dtype=np.float64), ct.c_double,

@@ -221,7 +221,7 @@ struct anacor_plan {
     int tiles = 0;
     int tile = kTile;              // voxels per work item
     int variant = 0;               // register-budget variant (0: process default)
-    bool morton = true;            // voxel list packed in Morton order
+    int order = 1;                 // voxel order of the packed list (0 the caller's, 1 Morton, 2.. blocked)
     long long *d_c64 = nullptr;    // the caller's int64 voxel list (for re-packing)
 };
 
@@ -250,7 +250,7 @@ void plan_release(anacor_plan *p)
 
 // Volume, tables and sizes of a plan (the voxel list comes next).
 int plan_init_volume(anacor_plan *p, const int8_t *label, const int64_t *shape, const double *voxel, const double *mu,
-                     int full, int is_exp, bool morton)
+                     int full, int is_exp, int order)
 {
     if (!label || !shape || !voxel || !mu)
         return fail(kErrArgs, "null argument");
@@ -269,7 +269,7 @@ int plan_init_volume(anacor_plan *p, const int8_t *label, const int64_t *shape, 
         p->mu[a] = mu[a];
     p->full = full;
     p->is_exp = is_exp;
-    p->morton = morton;
+    p->order = order;
     p->tile = kTile;
     cudaStream_t st = p->stream;
     const size_t nvol = (size_t)shape[0] * shape[1] * shape[2];
@@ -316,24 +316,23 @@ int plan_set_voxels(anacor_plan *p, const int64_t *coords, int64_t n, bool on_de
     if (n > 0) {
         if ((e = cudaMemcpyAsync(p->d_c64, coords, (size_t)n * 3 * sizeof(long long),
                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st)) ||
-            (e = p->morton ? launch_pack_coords_morton(p->d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)
-                           : launch_pack_coords(p->d_c64, (int)n, p->dims, p->d_coords, p->d_status, st)) ||
+            (e = launch_pack_coords_order(p->d_c64, (int)n, p->dims, p->order, p->d_coords, p->d_status, st)) ||
             (e = cudaStreamSynchronize(st)))
             return cuda_fail(e, "coordinate upload");
     }
     return kOk;
 }
 
-// `morton`: pack the voxel list in Morton order (A_h does not depend on the
-// order); per-voxel outputs keep the caller's order instead.
+// `order`: voxel order of the packed list (A_h does not depend on it; Morton
+// by default); per-voxel outputs keep the caller's order (0) instead.
 int plan_init(anacor_plan *p, const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
-              const double *voxel, const double *mu, int full, int is_exp, bool morton = true)
+              const double *voxel, const double *mu, int full, int is_exp, int order = 1)
 {
     if (!coords)
         return fail(kErrArgs, "null argument");
     if (n < 0 || n >= (1ll << 31))
         return fail(kErrArgs, "coordinate count out of range");
-    if (int st = plan_init_volume(p, label, shape, voxel, mu, full, is_exp, morton))
+    if (int st = plan_init_volume(p, label, shape, voxel, mu, full, is_exp, order))
         return st;
     return plan_set_voxels(p, coords, n, false);
 }
@@ -557,19 +556,19 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
 }
 
 
-int plan_configure(anacor_plan *p, int variant, int tile, int morton)
+int plan_configure(anacor_plan *p, int variant, int tile, int order)
 {
-    if (variant < 0 || variant > 4 || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) || morton < -1 ||
-        morton > 1)
+    if (variant < 0 || variant > 4 || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) || order < -1 ||
+        order >= kVoxelOrders)
         return fail(kErrArgs, "bad plan configuration");
     cudaError_t e;
-    if (morton >= 0 && (morton != 0) != p->morton && p->n_vox > 0) {
-        e = morton ? launch_pack_coords_morton(p->d_c64, p->n_vox, p->dims, p->d_coords, p->d_status, p->stream)
-                   : launch_pack_coords(p->d_c64, p->n_vox, p->dims, p->d_coords, p->d_status, p->stream);
+    if (order >= 0 && order != p->order && p->n_vox > 0) {
+        e = launch_pack_coords_order(p->d_c64, p->n_vox, p->dims, order, p->d_coords, p->d_status, p->stream);
         if (e)
             return cuda_fail(e, "voxel list packing");
-        p->morton = morton != 0;
     }
+    if (order >= 0)
+        p->order = order;
     if (tile) {
         p->tile = tile;
         p->tiles = (int)(((long long)p->n_vox + tile - 1) / tile);
@@ -616,7 +615,7 @@ struct TuneKey {
     }
 };
 struct TuneVal {
-    int variant, tile, morton;
+    int variant, tile, order;
     float ms;
 };
 std::map<TuneKey, TuneVal> g_tune_cache;
@@ -699,7 +698,7 @@ int plan_view(const anacor_plan *p, PlanView *v)
     v->n_vox = p->n_vox;
     v->coords = p->d_coords;
     v->c64 = p->d_c64;
-    v->morton = p->morton ? 1 : 0;
+    v->order = p->order;
     v->full_iteration = p->full;
     v->is_exp = p->is_exp;
     v->sq = p->d_sq;
@@ -762,7 +761,7 @@ anacor_plan *anacor_plan_create_sampled(const int8_t *label, const int64_t *shap
     }
     long long *d_c = nullptr;
     int64_t n = 0;
-    int st = plan_init_volume(p, label, shape, voxel, mu, full_iteration, is_exp, true);
+    int st = plan_init_volume(p, label, shape, voxel, mu, full_iteration, is_exp, 1);
     if (!st)
         st = sample_voxels_device(p, crystal_code, method, sampling_size, sampling_ratio, stride, &d_c, &n);
     if (!st)
@@ -1177,7 +1176,7 @@ int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *
         return fail(st, status_text(st));
     static const double mu0[4] = {0, 0, 0, 0};
     anacor_plan p;
-    int st = plan_init(&p, label, shape, coords, n, voxel, mu0, full_iteration, 1, false);
+    int st = plan_init(&p, label, shape, coords, n, voxel, mu0, full_iteration, 1, 0);
     ReflTable *d_tab = nullptr;
     double *d_vox = nullptr;
     int *d_i = nullptr;
@@ -1235,16 +1234,16 @@ int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *
 }
 
 
-int anacor_plan_configure(anacor_plan *p, int variant, int tile, int morton)
+int anacor_plan_configure(anacor_plan *p, int variant, int tile, int order)
 {
     if (!p)
         return fail(kErrArgs, "null plan");
-    if (int st = plan_configure(p, variant, tile, morton))
+    if (int st = plan_configure(p, variant, tile, order))
         return st;
     return succeed();
 }
 
-int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *morton)
+int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *order)
 {
     if (!p)
         return fail(kErrArgs, "null plan");
@@ -1252,8 +1251,8 @@ int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *morto
         *variant = p->variant ? p->variant : absorption_variant();
     if (tile)
         *tile = p->tile;
-    if (morton)
-        *morton = p->morton ? 1 : 0;
+    if (order)
+        *order = p->order;
     return succeed();
 }
 
@@ -1272,33 +1271,37 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
             const TuneVal v = it->second;
             if (best_ms)
                 *best_ms = v.ms;
-            return plan_configure(p, v.variant, v.tile, v.morton) ? t_status : succeed();
+            return plan_configure(p, v.variant, v.tile, v.order) ? t_status : succeed();
         }
     }
-    static const int variants[] = {2, 3, 4};
-    static const int tiles[] = {1024, 2048, 4096};
-    TuneVal best{0, 0, 0, 1e30f};
-    for (int morton = 1; morton >= 0; morton--) {
-        for (int tile : tiles) {
-            for (int variant : variants) {
-                if (int st = plan_configure(p, variant, tile, morton))
-                    return st;
-                // enough reflections for a few waves of work items
-                const long long slots = (long long)p->dev->sms * variant_occupancy(p->dev, variant);
-                int64_t k = (int64_t)((4 * slots + p->tiles - 1) / p->tiles);
-                if (sample_refl > 0)
-                    k = std::max<int64_t>(k, sample_refl);
-                k = std::min<int64_t>(k, p->n_refl);
-                float ms = 0.0f;
-                if (int st = plan_time(p, k, 2, &ms))
-                    return st;
-                ms = ms * (float)p->n_refl / (float)k;
-                if (ms < best.ms)
-                    best = TuneVal{variant, tile, morton, ms};
-            }
-        }
-    }
-    if (int st = plan_configure(p, best.variant, best.tile, best.morton))
+    // first the voxel order at the default variant and tile, then variant x tile with that order
+    TuneVal best{0, 0, 1, 1e30f};
+    auto trial = [&](int variant, int tile, int order) -> int {
+        if (int st = plan_configure(p, variant, tile, order))
+            return st;
+        // enough reflections for a few waves of work items
+        const long long slots = (long long)p->dev->sms * variant_occupancy(p->dev, variant);
+        int64_t k = (int64_t)((4 * slots + p->tiles - 1) / p->tiles);
+        if (sample_refl > 0)
+            k = std::max<int64_t>(k, sample_refl);
+        k = std::min<int64_t>(k, p->n_refl);
+        float ms = 0.0f;
+        if (int st = plan_time(p, k, 2, &ms))
+            return st;
+        ms = ms * (float)p->n_refl / (float)k;
+        if (ms < best.ms)
+            best = TuneVal{variant, tile, order, ms};
+        return kOk;
+    };
+    for (int order = 0; order < kVoxelOrders; order++)
+        if (int st = trial(0, kTile, order))
+            return st;
+    const int order = best.order;
+    for (int tile : {1024, 2048, 4096})
+        for (int variant : {2, 3, 4})
+            if (int st = trial(variant, tile, order))
+                return st;
+    if (int st = plan_configure(p, best.variant, best.tile, best.order))
         return st;
     {
         std::lock_guard<std::mutex> lk(g_mu);

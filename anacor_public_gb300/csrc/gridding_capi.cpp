@@ -192,7 +192,7 @@ struct anacor_gridding {
     Axis ta, pa;
     float *d_map = nullptr;
     long long ld = 0;
-    int *d_col = nullptr;          // packed voxel -> caller column (Morton plans)
+    int *d_col = nullptr;          // packed voxel -> caller column (reordered plans)
     std::vector<int> col;          // host copy
     int *d_status = nullptr;
     unsigned long long *d_counter = nullptr;
@@ -201,6 +201,8 @@ struct anacor_gridding {
     InterpRow *d_rows = nullptr;
     double *d_out = nullptr;
     long long rows_cap = 0;
+    long long n_prepared = 0;      // rows uploaded by anacor_gridding_prepare
+    int prepared_linear = 0;
     int map_grid = 0;
 };
 
@@ -355,9 +357,9 @@ anacor_gridding *anacor_gridding_create(anacor_plan *plan, int n_theta, int n_ph
         anacor_gridding_destroy(g);
         return nullptr;
     }
-    if (g->pv.morton && g->pv.n_vox > 0) {
+    if (g->pv.order && g->pv.n_vox > 0) {
         if ((e = dalloc(&g->d_col, (size_t)g->pv.n_vox)) ||
-            (e = launch_morton_permutation(g->pv.c64, g->pv.n_vox, g->pv.dims, g->d_col, st)) ||
+            (e = launch_order_permutation(g->pv.c64, g->pv.n_vox, g->pv.dims, g->pv.order, g->d_col, st)) ||
             (e = cudaStreamSynchronize(st))) {
             cuda_err(e);
             anacor_gridding_destroy(g);
@@ -543,6 +545,39 @@ int anacor_gridding_interpolate(anacor_gridding *g, const double *s1, const doub
         (e = launch_gridding_interp_f32(g->d_map, 1, g->ld, g->pv.n_vox, g->d_rows, n, method == 2, g->d_out, st)) ||
         (e = cudaMemcpyAsync(out, g->d_out, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, st)) ||
         (e = cudaStreamSynchronize(st)))
+        return cuda_err(e);
+    return report_status(kOk, "");
+}
+
+// Lookup rows of n reflections computed on the host and kept on the device,
+// so that anacor_gridding_run launches the interpolation alone.
+int anacor_gridding_prepare(anacor_gridding *g, const double *s1, const double *omega, int64_t n, const double *xray,
+                            const double *omega_axis, const double *F, int method)
+{
+    if (!g || n < 0 || (n > 0 && (!s1 || !omega || !xray || !omega_axis || !F)) || (method != 1 && method != 2))
+        return report_status(kErrArgs, "bad arguments");
+    std::vector<InterpRow> rows;
+    if (int st = interp_rows(g, s1, omega, n, xray, omega_axis, F, method == 2, rows))
+        return st;
+    if (int st = ensure_rows(g, n))
+        return st;
+    cudaError_t e;
+    if (n > 0 && ((e = cudaMemcpyAsync(g->d_rows, rows.data(), rows.size() * sizeof(InterpRow), cudaMemcpyHostToDevice,
+                                       g->pv.stream)) ||
+                  (e = cudaStreamSynchronize(g->pv.stream))))
+        return cuda_err(e);
+    g->n_prepared = n;
+    g->prepared_linear = method == 2;
+    return report_status(kOk, "");
+}
+
+int anacor_gridding_run(anacor_gridding *g, double *d_out, void *stream)
+{
+    if (!g || !d_out || !g->built || g->pv.n_vox == 0)
+        return report_status(kErrArgs, "bad arguments or no map");
+    cudaStream_t st = stream ? (cudaStream_t)stream : g->pv.stream;
+    if (cudaError_t e = launch_gridding_interp_f32(g->d_map, 1, g->ld, g->pv.n_vox, g->d_rows, g->n_prepared,
+                                                   g->prepared_linear, d_out, st))
         return cuda_err(e);
     return report_status(kOk, "");
 }

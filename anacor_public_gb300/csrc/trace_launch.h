@@ -73,7 +73,7 @@ struct PlanView {
     int n_vox;
     const short4 *coords;     // packed list (Morton order when morton)
     const long long *c64;     // the caller's (z, y, x) list, device
-    int morton;
+    int order;                // voxel order of `coords` (0: the caller's)
     int full_iteration, is_exp;
     double mu[4], voxel[3];
     const double *sq;
@@ -93,9 +93,12 @@ int absorption_variant();
 
 cudaError_t launch_pack_coords(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
                                cudaStream_t st);
-// Same, with the packed list sorted by the Morton code of (z, y, x).
-cudaError_t launch_pack_coords_morton(const long long *d_c, int n, const int *dims, short4 *d_out, int *d_status,
-                                      cudaStream_t st);
+// Voxel orders of the packed list: 0 the caller's, 1 Morton (Z-order) of
+// (z, y, x), 2 .. kVoxelOrders-1 blocked (Morton order of blocks, row order
+// inside a block; block shapes in voxel_order.cu).
+constexpr int kVoxelOrders = 8;
+cudaError_t launch_pack_coords_order(const long long *d_c, int n, const int *dims, int order, short4 *d_out,
+                                     int *d_status, cudaStream_t st);
 // Crystal-voxel sampling (sampling.cu): voxels with label == code (and, for
 // stride > 1, z, y, x multiples of stride) in C order as linear indices;
 // unravel_voxels writes (z, y, x) int64 of entry floor(j * step) (step > 0,
@@ -106,8 +109,9 @@ cudaError_t select_sampled_voxels(const int8_t *d_vol, const int *dims, int code
                                   long long *d_count, cudaStream_t st);
 cudaError_t unravel_voxels(const long long *d_lin, long long n_out, double step, const int *dims, long long *d_coords,
                            cudaStream_t st);
-// perm[k] = index in the caller's list of the k-th voxel of the Morton-packed list
-cudaError_t launch_morton_permutation(const long long *d_c, int n, const int *dims, int *d_perm, cudaStream_t st);
+// perm[k] = index in the caller's list of the k-th voxel of the packed list
+cudaError_t launch_order_permutation(const long long *d_c, int n, const int *dims, int order, int *d_perm,
+                                     cudaStream_t st);
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs
 // take items from `d_counter` (reset inside the launch sequence).
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,

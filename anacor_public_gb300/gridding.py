@@ -114,6 +114,18 @@ class GriddingMap:
                                                              ct.c_void_p(d_out), ct.c_void_p(stream or 0)),
                    self._L)
 
+    def prepare(self, s1, omega, xray, omega_axis, F, method: str | int = "nearest"):
+        """Compute and keep on the device the lookups of these reflections."""
+        m = {"nearest": 1, "linear": 2}.get(method, method)
+        s1 = _c(s1, np.float64).reshape(-1, 3)
+        _lib.check(self._L.anacor_gridding_prepare(self._h, s1, _c(omega, np.float64), s1.shape[0],
+                                                   _c(xray, np.float64), _c(omega_axis, np.float64),
+                                                   _c(F, np.float64).reshape(-1), int(m)), self._L)
+
+    def run(self, d_out: int, stream: int | None = None):
+        """Interpolation kernel over the prepared reflections into device d_out."""
+        _lib.check(self._L.anacor_gridding_run(self._h, ct.c_void_p(d_out), ct.c_void_p(stream or 0)), self._L)
+
     def close(self):
         if getattr(self, "_h", None):
             self._L.anacor_gridding_destroy(self._h)

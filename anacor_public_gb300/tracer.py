@@ -136,15 +136,15 @@ class Plan:
         _lib.check(self._L.anacor_plan_count_steps(self._h, ct.byref(n)), self._L)
         return int(n.value)
 
-    def configure(self, variant: int = 0, tile: int = 0, morton: int = -1):
+    def configure(self, variant: int = 0, tile: int = 0, order: int = -1):
         """Execution parameters: kernel register-budget variant (CTAs/SM), voxels
-        per work item, Morton voxel order (1) or the caller's order (0)."""
-        _lib.check(self._L.anacor_plan_configure(self._h, int(variant), int(tile), int(morton)), self._L)
+        per work item, voxel order (0 the caller's, 1 Morton, 2..7 blocked)."""
+        _lib.check(self._L.anacor_plan_configure(self._h, int(variant), int(tile), int(order)), self._L)
 
     def config(self) -> dict:
         v, t, m = ct.c_int(), ct.c_int(), ct.c_int()
         _lib.check(self._L.anacor_plan_config(self._h, ct.byref(v), ct.byref(t), ct.byref(m)), self._L)
-        return {"variant": v.value, "tile": t.value, "morton": m.value}
+        return {"variant": v.value, "tile": t.value, "order": m.value}
 
     def autotune(self, sample_refl: int = 0) -> float:
         """Pick the fastest (variant, tile, order) on a reflection sample; returns

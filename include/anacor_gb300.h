@@ -143,10 +143,12 @@ int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *c
  * not change the per-ray results, only the FP32 summation order of A_h):
  * variant = register-budget variant of the kernel, i.e. the CTAs per SM it is
  * compiled for (1..4, 0 = process default); tile = voxels per work item
- * (>= 512, 0 = unchanged); morton = 1 to pack the voxel list in Morton order,
- * 0 for the caller's order, -1 unchanged. */
-int anacor_plan_configure(anacor_plan *p, int variant, int tile, int morton);
-int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *morton);
+ * (>= 512, 0 = unchanged); order = voxel order of the packed list: 0 the
+ * caller's, 1 Morton (Z-order) of (z, y, x), 2..7 blocked (Morton order of
+ * blocks of 1x2x16, 1x4x8, 2x4x32, 4x8x64, 4x16x32 or 8x16x128 voxels, row
+ * order inside a block), -1 unchanged. */
+int anacor_plan_configure(anacor_plan *p, int variant, int tile, int order);
+int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *order);
 /* Autotuner: times every (variant, tile, order) candidate on the first
  * reflections of the plan (at least sample_refl of them) and keeps the
  * fastest; results are cached per volume shape and voxel-count class.
@@ -262,6 +264,11 @@ int anacor_gridding_interpolate(anacor_gridding *g, const double *s1, const doub
 int anacor_gridding_interpolate_async(anacor_gridding *g, const double *s1, const double *omega, int64_t n,
                                       const double *xray, const double *omega_axis, const double *F, int method,
                                       double *d_out, void *stream);
+/* The lookups of n reflections prepared once (host set-up, rows kept on the
+ * device), then the interpolation kernel alone into d_out[n] on `stream`. */
+int anacor_gridding_prepare(anacor_gridding *g, const double *s1, const double *omega, int64_t n, const double *xray,
+                            const double *omega_axis, const double *F, int method);
+int anacor_gridding_run(anacor_gridding *g, double *d_out, void *stream);
 void anacor_gridding_destroy(anacor_gridding *g);
 
 /* Drop-in for AnACor/src/ray_tracing.c:484-534 (bound at

@@ -149,3 +149,15 @@ def test_gridding_accuracy_vs_plain(small, built):
     el = np.abs(lin - plain) / plain
     # a 5-degree grid: percent-level approximations, bilinear better than nearest
     assert np.median(en) < 0.05 and np.median(el) < np.median(en)
+
+
+def test_prepare_run_equals_interpolate(small, built):
+    import torch
+    _, g, _ = built
+    n = small.n_refl
+    want = g.interpolate(small.s1, small.omega, small.xray, small.omega_axis, small.F, method=1)
+    g.prepare(small.s1, small.omega, small.xray, small.omega_axis, small.F, method=1)
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    g.run(d.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(d.cpu().numpy(), want)

@@ -29,11 +29,11 @@ def want(sample, oracle):
 
 @pytest.mark.parametrize("variant", [2, 3, 4])
 @pytest.mark.parametrize("tile", [512, 2048, 8192])
-@pytest.mark.parametrize("morton", [0, 1])
-def test_every_configuration_matches_the_oracle(sample, want, variant, tile, morton):
+@pytest.mark.parametrize("order", list(range(8)))
+def test_every_configuration_matches_the_oracle(sample, want, variant, tile, order):
     p = tracer.Plan.from_sample(sample)
-    p.configure(variant, tile, morton)
-    assert p.config() == {"variant": variant, "tile": tile, "morton": morton}
+    p.configure(variant, tile, order)
+    assert p.config() == {"variant": variant, "tile": tile, "order": order}
     p.run()
     a = p.result()
     p.run()

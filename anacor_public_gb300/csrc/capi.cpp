@@ -1276,31 +1276,51 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
     }
     // first the voxel order at the default variant and tile, then variant x tile with that order
     TuneVal best{0, 0, 1, 1e30f};
-    auto trial = [&](int variant, int tile, int order) -> int {
+    // time of one candidate (ms for all reflections): best of three runs over
+    // enough reflections for about eight waves of work items
+    auto timed = [&](int variant, int tile, int order, float &out) -> int {
         if (int st = plan_configure(p, variant, tile, order))
             return st;
-        // enough reflections for a few waves of work items
         const long long slots = (long long)p->dev->sms * variant_occupancy(p->dev, variant);
-        int64_t k = (int64_t)((4 * slots + p->tiles - 1) / p->tiles);
+        int64_t k = (int64_t)((8 * slots + p->tiles - 1) / p->tiles);
         if (sample_refl > 0)
             k = std::max<int64_t>(k, sample_refl);
         k = std::min<int64_t>(k, p->n_refl);
-        float ms = 0.0f;
-        if (int st = plan_time(p, k, 2, &ms))
-            return st;
-        ms = ms * (float)p->n_refl / (float)k;
-        if (ms < best.ms)
-            best = TuneVal{variant, tile, order, ms};
+        out = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+            float ms = 0.0f;
+            if (int st = plan_time(p, k, 1, &ms))
+                return st;
+            out = std::min(out, ms * (float)p->n_refl / (float)k);
+        }
         return kOk;
     };
-    for (int order = 0; order < kVoxelOrders; order++)
-        if (int st = trial(0, kTile, order))
+    // voxel order first: Morton unless another order is clearly faster (the
+    // differences between orders are small and the sample is short)
+    float t_ref = 0.0f;
+    if (int st = timed(0, kTile, 1, t_ref))
+        return st;
+    int order = 1;
+    float t_order = t_ref;
+    for (int o = 0; o < kVoxelOrders; o++) {
+        if (o == 1)
+            continue;
+        float t = 0.0f;
+        if (int st = timed(0, kTile, o, t))
             return st;
-    const int order = best.order;
+        if (t < 0.97f * t_ref && t < t_order) {
+            order = o;
+            t_order = t;
+        }
+    }
     for (int tile : {1024, 2048, 4096})
-        for (int variant : {2, 3, 4})
-            if (int st = trial(variant, tile, order))
+        for (int variant : {2, 3, 4}) {
+            float t = 0.0f;
+            if (int st = timed(variant, tile, order, t))
                 return st;
+            if (t < best.ms)
+                best = TuneVal{variant, tile, order, t};
+        }
     if (int st = plan_configure(p, best.variant, best.tile, best.order))
         return st;
     {

@@ -20,14 +20,16 @@
 //              boundary are recomputed with the reference's FP64 expression.
 //              Lanes that may touch a volume wall, faces with ratios beyond
 //              fixed-point range and full_iteration march per lane in FP64.
-//   lengths    (cal_path2_plus, :1462-1552): FP64, same operation order; the
-//              per-segment quotient fl(span / (len-1)) comes from a table of
-//              correctly rounded quotients, or from a correctly rounded
-//              reciprocal and one FMA correction (exhaustively checked).
-//   rate       (cal_rate, :1554-1583): FP64 exponent, exp in FP32 after an
-//              FP64 range reduction; per-thread Neumaier sums, warp-shuffle
-//              TwoSum reduction, tile partials combined in FP64 in a fixed
-//              order (deterministic for any schedule).
+//   lengths    (cal_path2_plus, :1462-1552): for A_h in FP32 (the segments and
+//              len_path_2 come from the exact march; A_h needs 1e-6); for the
+//              per-voxel detail and the gridding map in FP64 with the
+//              reference's operation order, the per-segment quotient
+//              fl(span / (len-1)) from a table of correctly rounded quotients,
+//              or a correctly rounded reciprocal and one FMA correction.
+//   rate       (cal_rate, :1554-1583): FP32 exponent and exp; per-thread
+//              Neumaier sums, warp-shuffle TwoSum reduction, tile partials
+//              combined in FP64 in a fixed order (deterministic for any
+//              schedule).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -308,7 +310,8 @@ __device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, 
 }
 
 struct LegResult {
-    double L[4];
+    double L[4];       // FP64 lengths (kF32 == false)
+    float Lf[4];       // FP32 lengths (kF32 == true)
     int face, len, nseg, status;
     int first[3], last[3];
 };
@@ -335,7 +338,10 @@ __device__ __forceinline__ double sq_len(const double *sq, int stride, int axis,
 // its increments (both end points at least one voxel inside the volume) and
 // the face has fixed-point ratios; other lanes, and full_iteration, use the
 // per-lane march.
-template <bool kDetail>
+// kF32: the per-class lengths in FP32 (for A_h, which needs 1e-6; the march
+// itself, and hence the visited voxels, segments and len_path_2, is the same);
+// otherwise FP64 in the reference's order (bit-exact lengths).
+template <bool kDetail, bool kF32 = false>
 __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
                                           bool valid, const Vol &v, int full, const double *voxel,
                                           const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
@@ -343,6 +349,7 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
 {
     const int lane = threadIdx.x & 31;
     out.L[0] = out.L[1] = out.L[2] = out.L[3] = 0.0;
+    out.Lf[0] = out.Lf[1] = out.Lf[2] = out.Lf[3] = 0.0f;
     out.len = 1; out.nseg = 1; out.status = kOk;
     if (kDetail) {
         out.first[0] = cz; out.first[1] = cy; out.first[2] = cx;
@@ -541,6 +548,28 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         if (len == 1)
             return;
     }
+    if (kF32 && m.nseg <= kMaxSegments) {
+        // total and segment fractions in FP32: tot * (span / (len - 1))
+        const float ty = __fmul_rn((float)abs(ly - fy), (float)voxel[1]);
+        const float tz = __fmul_rn((float)abs(lz - fz), (float)voxel[0]);
+        const float tx = __fmul_rn((float)abs(lx - fx), (float)voxel[2]);
+        const float totf = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ty, ty), __fmul_rn(tz, tz)), __fmul_rn(tx, tx)));
+        const float scale = __fdiv_rn(totf, (float)(len - 1));
+        int cur = seg[0];
+        for (int j = 0; j < m.nseg; j++) {
+            const int nxt = (j + 1 < m.nseg) ? (int)seg[(j + 1) * kBlock] : -1;
+            const int start = cur & 0x1fff;
+            const int end = (j + 1 < m.nseg) ? (nxt & 0x1fff) : len;
+            const int cls = cur >> 13;
+            const float term = scale * (float)(end - start);
+            out.Lf[0] += cls == 1 ? term : 0.0f;
+            out.Lf[1] += cls == 2 ? term : 0.0f;
+            out.Lf[2] += cls == 3 ? term : 0.0f;
+            out.Lf[3] += cls == 4 ? term : 0.0f;
+            cur = nxt;
+        }
+        return;
+    }
     // total from the first and last path points, y then z then x
     const double yy = sq_len(sq, sq_stride, 1, abs(ly - fy), voxel[1]);
     const double zz = sq_len(sq, sq_stride, 0, abs(lz - fz), voxel[0]);
@@ -572,8 +601,10 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         march_lane<1>(R, g, cz, cy, cx, steps, v, full, m2, s2);
         const double q = seg_quotient(qtab, den_i, len - s2.open_pos, dr.x, dr.y);
         add_class(s2.open_cls, __dmul_rn(tot, q), s2.seen, s2.L);
-        for (int k = 0; k < 4; k++)
+        for (int k = 0; k < 4; k++) {
             out.L[k] = s2.L[k];
+            out.Lf[k] = (float)s2.L[k];
+        }
     }
 }
 
@@ -645,7 +676,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
 {
     __shared__ ReflTable tab;
     __shared__ uint16_t seg[kMaxSegments * kBlock];
-    __shared__ double lsum[4][kBlock];
+    __shared__ float lsum[4][kBlock];
     __shared__ float red_s[kWarps], red_c[kWarps];
     __shared__ long long item_s;
     __shared__ int last_s;
@@ -675,6 +706,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         float s = 0.0f, c = 0.0f;
         int bad = kOk;
         unsigned nsteps = 0;
+        const float muf[4] = {(float)D.mu[0], (float)D.mu[1], (float)D.mu[2], (float)D.mu[3]};
         const int v0 = t * D.tile;
         const int v1 = min(D.n_vox, v0 + D.tile);
         // every lane runs the same number of iterations (the march is warp-synchronous)
@@ -685,8 +717,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
 #pragma unroll 1
             for (int leg = 0; leg < 2; leg++) {
                 LegResult a;
-                trace_leg<false>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v, D.full_iteration,
-                                 D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
+                trace_leg<false, true>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v,
+                                       D.full_iteration, D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
                 bad |= a.status;
                 nsteps += valid ? (unsigned)a.len : 0u;
                 // the incident leg's lengths wait in shared memory while the
@@ -694,16 +726,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
                 // class, as cal_rate adds them
 #pragma unroll
                 for (int k = 0; k < 4; k++)
-                    lsum[k][tid] = leg == 0 ? a.L[k] : __dadd_rn(lsum[k][tid], a.L[k]);
+                    lsum[k][tid] = leg == 0 ? a.Lf[k] : lsum[k][tid] + a.Lf[k];
             }
             if (valid) {
-                // cal_rate's exponent, operand order of AnACor/src/ray_tracing_basic.c:1573-1576
-                const double t0 = __dmul_rn(D.mu[0], lsum[0][tid]);
-                const double t1 = __dmul_rn(D.mu[1], lsum[1][tid]);
-                const double t2 = __dmul_rn(D.mu[2], lsum[2][tid]);
-                const double t3 = __dmul_rn(D.mu[3], lsum[3][tid]);
-                const double ex = __dadd_rn(__dadd_rn(__dadd_rn(t0, t1), t2), t3);
-                const float term = D.is_exp ? exp_neg(ex) : (float)ex;
+                // cal_rate's exponent (AnACor/src/ray_tracing_basic.c:1573-1576), in FP32
+                const float ex = muf[0] * lsum[0][tid] + muf[1] * lsum[1][tid] + muf[2] * lsum[2][tid] +
+                                 muf[3] * lsum[3][tid];
+                const float term = D.is_exp ? expf(-ex) : ex;
                 float ns, e;
                 two_sum(s, term, ns, e);
                 s = ns;

@@ -218,6 +218,7 @@ struct anacor_plan {
     const double *d_qtab = nullptr;  // device quotient table (owned by the device state)
     ReflTable *h_refl = nullptr;   // pinned staging
     int64_t n_refl = 0, refl_cap = 0;
+    size_t partial_cap = 0;        // entries of d_partial (refl_cap * tiles)
     int tiles = 0;
     int tile = kTile;              // voxels per work item
     int variant = 0;               // register-budget variant (0: process default)
@@ -246,6 +247,16 @@ void plan_release(anacor_plan *p)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
     cudaStreamSynchronize(st);
+}
+
+// the tile actually used: at least `tile`, and large enough that a reflection
+// has at most kMaxTilesPerRefl tiles (a multiple of 32 voxels)
+int effective_tile(int n_vox, int tile)
+{
+    const long long need = ((long long)n_vox + kMaxTilesPerRefl - 1) / kMaxTilesPerRefl;
+    if (need > tile)
+        tile = (int)((need + 31) / 32 * 32);
+    return tile;
 }
 
 // Volume, tables and sizes of a plan (the voxel list comes next).
@@ -309,6 +320,7 @@ int plan_set_voxels(anacor_plan *p, const int64_t *coords, int64_t n, bool on_de
     dev_free(p->d_coords, st);
     dev_free(p->d_c64, st);
     p->n_vox = (int)n;
+    p->tile = effective_tile(p->n_vox, p->tile);
     p->tiles = (int)((n + p->tile - 1) / p->tile);
     cudaError_t e;
     if ((e = dev_alloc(&p->d_coords, (size_t)n, st)) || (e = dev_alloc(&p->d_c64, (size_t)n * 3, st)))
@@ -383,6 +395,21 @@ int sample_voxels_device(anacor_plan *p, int code, int method, int64_t sampling_
     return kOk;
 }
 
+// tile partial sums: one per (reflection, tile) for the reserved reflections
+int plan_ensure_partial(anacor_plan *p)
+{
+    const size_t need = (size_t)p->refl_cap * (size_t)std::max(1, p->tiles);
+    if (need <= p->partial_cap)
+        return kOk;
+    cudaStream_t st = p->stream;
+    dev_free(p->d_partial, st);
+    p->partial_cap = 0;
+    if (cudaError_t e = dev_alloc(&p->d_partial, need, st))
+        return cuda_fail(e, "device allocation");
+    p->partial_cap = need;
+    return kOk;
+}
+
 int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
 {
     cudaStream_t st = p->stream;
@@ -397,9 +424,8 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
             cudaFreeHost(p->h_refl);
             p->h_refl = nullptr;
         }
+        p->partial_cap = 0;
         if ((e = dev_alloc(&p->d_refl, (size_t)n_refl, st)) || (e = dev_alloc(&p->d_out, (size_t)n_refl, st)) ||
-            (e = dev_alloc(&p->d_partial,
-                           (size_t)n_refl * (size_t)std::max(1, (p->n_vox + kMinTile - 1) / kMinTile), st)) ||
             (e = dev_alloc(&p->d_arrive, (size_t)n_refl, st)))
             return cuda_fail(e, "device allocation");
         if ((e = cudaMemsetAsync(p->d_arrive, 0, (size_t)n_refl * sizeof(unsigned), st)))
@@ -409,7 +435,7 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
         p->refl_cap = n_refl;
     }
     p->n_refl = n_refl;
-    return kOk;
+    return plan_ensure_partial(p);
 }
 
 SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
@@ -570,8 +596,10 @@ int plan_configure(anacor_plan *p, int variant, int tile, int order)
     if (order >= 0)
         p->order = order;
     if (tile) {
-        p->tile = tile;
-        p->tiles = (int)(((long long)p->n_vox + tile - 1) / tile);
+        p->tile = effective_tile(p->n_vox, tile);
+        p->tiles = (int)(((long long)p->n_vox + p->tile - 1) / p->tile);
+        if (int st = plan_ensure_partial(p))
+            return st;
     }
     p->variant = variant;
     return plan_upload_desc(p, nullptr);
@@ -1276,7 +1304,7 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
     }
     // first the voxel order at the default variant and tile, then variant x tile with that order
     TuneVal best{0, 0, 1, 1e30f};
-    // time of one candidate (ms for all reflections): best of three runs over
+    // time of one candidate (ms for all reflections): best of five runs over
     // enough reflections for about eight waves of work items
     auto timed = [&](int variant, int tile, int order, float &out) -> int {
         if (int st = plan_configure(p, variant, tile, order))
@@ -1287,7 +1315,7 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
             k = std::max<int64_t>(k, sample_refl);
         k = std::min<int64_t>(k, p->n_refl);
         out = 1e30f;
-        for (int rep = 0; rep < 3; rep++) {
+        for (int rep = 0; rep < 5; rep++) {
             float ms = 0.0f;
             if (int st = plan_time(p, k, 1, &ms))
                 return st;
@@ -1313,7 +1341,7 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
             t_order = t;
         }
     }
-    for (int tile : {1024, 2048, 4096})
+    for (int tile : {128, 256, 512, 1024, 2048})
         for (int variant : {2, 3, 4}) {
             float t = 0.0f;
             if (int st = timed(variant, tile, order, t))

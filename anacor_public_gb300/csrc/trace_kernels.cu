@@ -1,9 +1,10 @@
 // sm_103a kernels of the absorption-factor path.
 //
-// One CTA processes one work item = (sample, reflection, tile of kTile
-// consecutive coordinate-list voxels).  Thread k of the CTA takes voxels
-// tile*kTile + k + j*kBlock, so the 32 lanes of a warp hold 32 adjacent
-// crystal voxels (np.where order: adjacent x) and march them along the same
+// One warp processes one work item = (sample, reflection, tile of consecutive
+// voxels of the packed list) taken from an atomic counter, so a warp that
+// finishes early takes the next item instead of waiting for its CTA.  Lane k
+// takes voxels tile*t + k + 32*j: the 32 lanes hold 32 consecutive entries of
+// the Morton-ordered list (a compact 3-D block) and march them along the same
 // two directions.
 //
 // Per voxel (the body of AnACor/src/ray_tracing.c:199-278), per leg:
@@ -674,19 +675,17 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
                                                                         int n_desc, long long total_items,
                                                                         unsigned long long *__restrict__ work_counter)
 {
-    __shared__ ReflTable tab;
+    __shared__ ReflTable tabs[kWarps];   // one per warp: items are taken per warp
     __shared__ uint16_t seg[kMaxSegments * kBlock];
     __shared__ float lsum[4][kBlock];
-    __shared__ float red_s[kWarps], red_c[kWarps];
-    __shared__ long long item_s;
-    __shared__ int last_s;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    ReflTable &tab = tabs[warp];
     for (;;) {
-        if (tid == 0)
-            item_s = (long long)atomicAdd(work_counter, 1ull);
-        __syncthreads();
-        const long long item = item_s;
+        unsigned long long it = 0;
+        if (lane == 0)
+            it = atomicAdd(work_counter, 1ull);
+        const long long item = (long long)__shfl_sync(kAll, it, 0);
         if (item >= total_items)
             break;
         const int si = find_sample(descs, n_desc, item);
@@ -694,13 +693,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         const long long local = item - D.work_begin;
         const long long r = local / D.tiles;
         const int t = (int)(local - r * D.tiles);
+        __syncwarp();   // the previous item's reads of the table are done
         {
             const int4 *src = reinterpret_cast<const int4 *>(D.refl + r);
             int4 *dst = reinterpret_cast<int4 *>(&tab);
-            for (int k = tid; k < (int)(sizeof(ReflTable) / 16); k += kBlock)
+            for (int k = lane; k < (int)(sizeof(ReflTable) / 16); k += 32)
                 dst[k] = __ldg(src + k);
         }
-        __syncthreads();
+        __syncwarp();
 
         const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2]};
         float s = 0.0f, c = 0.0f;
@@ -710,8 +710,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         const int v0 = t * D.tile;
         const int v1 = min(D.n_vox, v0 + D.tile);
         // every lane runs the same number of iterations (the march is warp-synchronous)
-        for (int vb = v0; vb < v1; vb += kBlock) {
-            const int vi = vb + tid;
+        for (int vb = v0; vb < v1; vb += 32) {
+            const int vi = vb + lane;
             const bool valid = vi < v1;
             const short4 cv = valid ? __ldg(D.coords + vi) : make_short4(0, 0, 0, 0);
 #pragma unroll 1
@@ -749,7 +749,37 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             if (lane == 0)
                 atomicAdd(D.steps, w);
         }
-        finish_item(s, c, D, r, t, red_s, red_c, last_s);
+        // warp TwoSum reduction, the item's partial, and the fixed-order
+        // combination of the reflection's partials by the last item to arrive
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float so = __shfl_down_sync(kAll, s, o);
+            const float co = __shfl_down_sync(kAll, c, o);
+            float ns, e;
+            two_sum(s, so, ns, e);
+            s = ns;
+            c = c + co + e;
+        }
+        int last = 0;
+        if (lane == 0) {
+            D.partial[r * D.tiles + t] = (double)s + (double)c;
+            __threadfence();
+            last = atomicAdd(D.arrive + r, 1u) == (unsigned)(D.tiles - 1);
+        }
+        if (__shfl_sync(kAll, last, 0)) {
+            __threadfence();
+            const volatile double *pp = D.partial + r * D.tiles;
+            double acc = 0.0;
+            for (int k = lane; k < D.tiles; k += 32)
+                acc += pp[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_down_sync(kAll, acc, o);
+            if (lane == 0) {
+                D.out[r] = acc / (double)D.n_vox;
+                D.arrive[r] = 0u;   // ready for the next launch
+            }
+        }
     }
 }
 

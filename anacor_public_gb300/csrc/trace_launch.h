@@ -9,10 +9,14 @@ struct anacor_plan;
 
 namespace anacor {
 
-// Voxels per work item (one CTA pass) unless a sample sets its own: a sample
-// with N voxels and R reflections is R * ceil(N / tile) work items.
+// Voxels per work item unless a sample sets its own: a sample with N voxels
+// and R reflections is R * ceil(N / tile) work items (taken per warp by the
+// absorption kernel, per CTA by the map and bisection kernels).
 constexpr int kTile = 2048;
-constexpr int kMinTile = 512;
+constexpr int kMinTile = 128;
+// A plan's tile is raised where needed so that a reflection has at most this
+// many tiles (bounds the per-(reflection, tile) partial sums).
+constexpr int kMaxTilesPerRefl = 4096;
 
 // One sample (volume + voxel list + reflections) of a launch.  All pointers
 // are device pointers.

@@ -143,7 +143,7 @@ int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *c
  * not change the per-ray results, only the FP32 summation order of A_h):
  * variant = register-budget variant of the kernel, i.e. the CTAs per SM it is
  * compiled for (1..4, 0 = process default); tile = voxels per work item
- * (>= 512, 0 = unchanged); order = voxel order of the packed list: 0 the
+ * (>= 128, 0 = unchanged); order = voxel order of the packed list: 0 the
  * caller's, 1 Morton (Z-order) of (z, y, x), 2..7 blocked (Morton order of
  * blocks of 1x2x16, 1x4x8, 2x4x32, 4x8x64, 4x16x32 or 8x16x128 voxels, row
  * order inside a block), -1 unchanged. */

@@ -267,18 +267,34 @@ __device__ __forceinline__ void point_at(const FaceRule &R, const LegGeom &g, in
 }
 
 // Per-lane march (cal_coord) for the lanes the cooperative march does not
-// take: walls within reach, huge ratios, full_iteration; and the second pass.
+// take: walls within reach, huge ratios, full_iteration; the second pass; and
+// (i_begin > 0) the increments after the cooperative part of a leg that did
+// not stop before the cooperative march's wall limit, continuing `m`.
+//
+// Out of line, with everything it needs passed by value or recomputed: a
+// by-reference argument whose object lives in the caller's registers would
+// move that object to the stack for the whole of the caller.
 template <int kMode>
-__device__ __noinline__ void march_lane(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx, int steps,
-                                        const Vol &v, int full, March &m, Sink &sk)
+__device__ __noinline__ void march_lane(const FaceRule &R, int cz, int cy, int cx, int steps, const Vol v, int full,
+                                        March &m, Sink &sk, int i_begin = 0)
 {
+    LegGeom g;
+    leg_geom(R, cz, cy, cx, v, g);
+    const int sz = v.dy * v.dx, sy = v.dx;
+    int z, y, x;
+    if (i_begin > 0) {
+        for (int i = i_begin; i < steps; i++) {
+            point_at(R, g, i, cz, cy, cx, v, z, y, x);
+            if (!visit<kMode>(m, sk, i, __ldg(v.p + (z * sz + y * sy + x)), full, R.vac_limit))
+                return;
+        }
+        return;
+    }
     m.last_i = 0; m.nseg = 1; m.vac = 0;
     if (kMode == 0)
         sk.seg[0] = (uint16_t)(3 << 13);
     if (steps <= 0)
         return;
-    const int sz = v.dy * v.dx, sy = v.dx;
-    int z, y, x;
     point_at(R, g, 0, cz, cy, cx, v, z, y, x);
     const int lab = __ldg(v.p + (z * sz + y * sy + x));
     if (!full) {
@@ -299,7 +315,7 @@ __device__ __noinline__ void march_lane(const FaceRule &R, const LegGeom &g, int
 
 // Label of increment `inc` from the reference's FP64 expression (an
 // increment whose fixed-point fraction lies near a rounding boundary).
-__device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol &v)
+__device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol v)
 {
     int pz, py, px;
     const int s = G.count_axis;
@@ -308,6 +324,25 @@ __device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, 
     py = s == 1 ? cy + inc * ds : exact_axis(cy, inc, G.q[1], G.use_round, v.dy);
     px = s == 2 ? cx + inc * ds : exact_axis(cx, inc, G.q[2], G.use_round, v.dx);
     return (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(v.p) + (pz * v.dy + py) * v.dx + px);
+}
+
+// Increments i >= 0 for which c + i*q stays at least 2 voxels inside [0, h]
+// (an estimate in FP32 with a margin; -1 when increment 0 is already too
+// close).  The cooperative march's end-point test decides; this only picks
+// the end point.
+__device__ __forceinline__ int wall_increments(double q, int c, int h)
+{
+    const float qf = (float)q;
+    float k;
+    if (qf > 0.0f)
+        k = __fdiv_rn((float)(h - 2 - c), qf);
+    else if (qf < 0.0f)
+        k = __fdiv_rn((float)(c - 2), -qf);
+    else
+        return (c >= 1 && c <= h - 1) ? 0x3fffffff : -1;
+    if (!(k >= 0.0f))
+        return -1;
+    return (int)fminf(floorf(k * 0.9999f), 1.0e9f);
 }
 
 struct LegResult {
@@ -387,12 +422,27 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         // taken separately after the cooperative part
         const int steps_eff = R.count_kind == 2 ? steps - 1 : steps;
         coop = R.fast && !full && steps >= 1;
+        lim = steps_eff;
         if (coop && steps_eff > 1) {
-            const long long ena = g.off + (long long)(steps_eff - 1) * g.Qa;
-            const long long enb = g.off + (long long)(steps_eff - 1) * g.Qb;
-            const int a1 = g.ca + (int)((g.off + g.Qa) >> 32), an = g.ca + (int)(ena >> 32);
-            const int b1 = g.cb + (int)((g.off + g.Qb) >> 32), bn = g.cb + (int)(enb >> 32);
-            coop = min(a1, an) >= 1 && max(a1, an) <= g.ha - 1 && min(b1, bn) >= 1 && max(b1, bn) <= g.hb - 1;
+            // No increment of the cooperative part may clamp: its first and last
+            // points (the path is monotone on every axis) lie at least one voxel
+            // inside the volume.  When the volume's far wall is within reach of
+            // the full leg, the cooperative part ends at the last increment that
+            // stays clear of it; a leg still running there continues per lane.
+            int kend = steps_eff - 1;
+            for (int pass = 0; pass < 2; pass++) {
+                const long long ena = g.off + (long long)kend * g.Qa;
+                const long long enb = g.off + (long long)kend * g.Qb;
+                const int a1 = g.ca + (int)((g.off + g.Qa) >> 32), an = g.ca + (int)(ena >> 32);
+                const int b1 = g.cb + (int)((g.off + g.Qb) >> 32), bn = g.cb + (int)(enb >> 32);
+                coop = min(a1, an) >= 1 && max(a1, an) <= g.ha - 1 && min(b1, bn) >= 1 && max(b1, bn) <= g.hb - 1;
+                if (coop || pass == 1)
+                    break;
+                kend = min(kend, min(wall_increments(R.q[g.ia], g.ca, g.ha), wall_increments(R.q[g.ib], g.cb, g.hb)));
+                if (kend < 1)
+                    break;
+            }
+            lim = kend + 1;
         }
         if (coop) {
             base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
@@ -402,8 +452,7 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
                 stopped = true;
             } else {
                 m.prev = lab0;
-                live = steps_eff > 1;
-                lim = steps_eff;
+                live = lim > 1;
             }
         }
     }
@@ -457,6 +506,7 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
                 const unsigned amb_here = (ambm >> t) & ((1u << kMarchBatch) - 1u);
                 if (amb_here) {
                     // the reference's FP64 expression decides, per lane (c enters its rounding)
+#pragma unroll
                     for (int k = 0; k < kMarchBatch; k++)
                         if (((amb_here >> k) & 1u) && k < n)
                             lb[k] = exact_label(G, cz, cy, cx, ib + k, v);
@@ -520,7 +570,14 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
     const int cc = pick3(R.count_axis, cz, cy, cx);
     const int dd = pick3(R.count_axis, v.dz, v.dy, v.dx);
     const int steps = R.count_kind == 0 ? cc + 1 : (R.count_kind == 1 ? dd - cc : dd - cc + 1);
-    if (coop && !stopped && R.count_kind == 2) {
+    if (coop && !stopped && lim < (R.count_kind == 2 ? steps - 1 : steps)) {
+        // the cooperative part ended at the wall limit: the rest per lane
+        March mc = m;
+        Sink sc;
+        sc.seg = seg;
+        march_lane<0>(R, cz, cy, cx, steps, v, full, mc, sc, lim);
+        m = mc;
+    } else if (coop && !stopped && R.count_kind == 2) {
         // the clamped last increment of a count_kind 2 face
         int pz, py, px;
         const int inc = steps - 1;
@@ -529,8 +586,14 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         if (inc >= 1)
             visit<0>(m, sk, inc, lab, 0, R.vac_limit);
     }
-    if (!coop)
-        march_lane<0>(R, g, cz, cy, cx, steps, v, full, m, sk);
+    if (!coop) {
+        // separate objects for the out-of-line call (see march_lane)
+        March mc = m;
+        Sink sc;
+        sc.seg = seg;
+        march_lane<0>(R, cz, cy, cx, steps, v, full, mc, sc);
+        m = mc;
+    }
 
     // ---- cal_path2_plus
     const int len = m.last_i + 1;
@@ -599,7 +662,7 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         s2.tot = tot; s2.den = dr.x; s2.rcp = dr.y; s2.den_i = den_i;
         s2.L[0] = s2.L[1] = s2.L[2] = s2.L[3] = 0.0;
         s2.open_cls = 3; s2.open_pos = 0; s2.seen = 0;
-        march_lane<1>(R, g, cz, cy, cx, steps, v, full, m2, s2);
+        march_lane<1>(R, cz, cy, cx, steps, v, full, m2, s2);
         const double q = seg_quotient(qtab, den_i, len - s2.open_pos, dr.x, dr.y);
         add_class(s2.open_cls, __dmul_rn(tot, q), s2.seen, s2.L);
         for (int k = 0; k < 4; k++) {

@@ -263,6 +263,41 @@ def train_for_sample(s: synth.Sample, n_train: int = 100_000, steps: int = 20_00
     return model, loss
 
 
+def select_fourier_scale(x7: np.ndarray, log_ah: np.ndarray, candidates=(0.25, 0.35, 0.5),
+                         steps: int = 3000, batch: int = 4096, members: int = 4, seed: int = 0,
+                         lr_max: float = 3e-3, holdout: float = 0.1, spread_threshold: float = 1e-3):
+    """Fourier feature scale for a training set, chosen on held-out rows.
+
+    Each candidate ensemble trains for a short cosine schedule on all but the
+    last ``holdout`` fraction of the rows; the held-out rows are predicted and
+    the candidate with the fewest rows above ``spread_threshold`` (the rows the
+    audit would re-trace) wins, ties broken by the median relative error.
+    Returns (scale, {scale: (fallback fraction, median error)}).  A smaller
+    scale gives smoother features: it wins on strongly absorbing samples,
+    whose A_h varies more steeply with direction, where a larger scale
+    leaves the members disagreeing on more rows."""
+    x7 = _c(x7, np.float32).reshape(-1, 7)
+    log_ah = _c(log_ah, np.float64)
+    n = x7.shape[0]
+    n_fit = max(1, int(round(n * (1.0 - holdout))))
+    if n_fit >= n:
+        raise ValueError("select_fourier_scale needs held-out rows")
+    target = np.exp(log_ah[n_fit:])
+    scores = {}
+    for fs in candidates:
+        m = Surrogate(members=members, seed=seed, fourier_scale=float(fs))
+        try:
+            m.set_data(x7[:n_fit], log_ah[:n_fit])
+            m.train(steps, batch=batch, lr_max=lr_max, lr_min=lr_max * 1e-2, total_steps=steps)
+            mean, spread = m.predict(x7[n_fit:])
+        finally:
+            m.close()
+        fb = float(np.mean(~(spread <= spread_threshold)))
+        scores[float(fs)] = (fb, float(np.median(relative_error(mean, target))))
+    best = min(scores, key=lambda k: scores[k])
+    return best, scores
+
+
 def relative_error(a, b) -> np.ndarray:
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
@@ -270,5 +305,5 @@ def relative_error(a, b) -> np.ndarray:
 
 
 __all__ = ["Surrogate", "inputs", "sample_inputs", "tc_gemm", "training_set", "audited_absorption",
-           "AuditResult", "train_for_sample", "audit_flags", "audit_flags_host", "relative_error",
+           "AuditResult", "train_for_sample", "select_fourier_scale", "audit_flags", "audit_flags_host", "relative_error",
            "N_FEATURES", "WIDTH", "DEPTH"]

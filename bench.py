@@ -76,7 +76,8 @@ def parse():
     ap.add_argument("--train-steps", type=int, default=20000, help="surrogate: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096)
     ap.add_argument("--members", type=int, default=4)
-    ap.add_argument("--fourier-scale", type=float, default=0.5)
+    ap.add_argument("--fourier-scale", default="auto",
+                    help="surrogate Fourier feature scale, or 'auto' (chosen on held-out training rows)")
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--audit", type=float, default=0.02)
     ap.add_argument("--spread", type=float, default=1e-3)
@@ -495,7 +496,14 @@ def run_surrogate(args):
     trace_ms = e0.elapsed_time(e1)
     plain_rate = args.train_refl / (trace_ms / 1e3)
     x7_t = surrogate.inputs(om_t, s1_t, s.xray, s.omega_axis, s.F)
-    model = surrogate.Surrogate(members=args.members, seed=1 + rank, fourier_scale=args.fourier_scale)
+    t0 = time.perf_counter()
+    if args.fourier_scale == "auto":
+        fscale, fscores = surrogate.select_fourier_scale(x7_t, np.log(ah_t), members=args.members, seed=1 + rank,
+                                                         lr_max=args.lr, spread_threshold=args.spread)
+    else:
+        fscale, fscores = float(args.fourier_scale), {}
+    select_s = time.perf_counter() - t0
+    model = surrogate.Surrogate(members=args.members, seed=1 + rank, fourier_scale=fscale)
     model.set_data(x7_t, np.log(ah_t))
     t0 = time.perf_counter()
     loss = model.train(args.train_steps, batch=args.train_batch, lr_max=args.lr, lr_min=args.lr * 1e-2,
@@ -633,7 +641,9 @@ def run_surrogate(args):
                        "l2": "flushed between steps (256 MiB write)", "tuned": tuned},
             "plain_refl_per_s": plain_rate,
             "speedup_vs_plain": value / plain_rate,
-            "surrogate": {"train_s": train_s, "train_trace_s": trace_ms / 1e3,
+            "surrogate": {"train_s": train_s, "train_trace_s": trace_ms / 1e3, "fourier_scale": fscale,
+                          "scale_selection_s": select_s,
+                          "scale_scores": {str(k): {"fallback": v[0], "median_err": v[1]} for k, v in fscores.items()},
                           "final_loss": float(np.mean(loss[-100:])), "first_loss": float(np.mean(loss[:10])),
                           "fallback_fraction": float(np.mean(fallback)), "traced_per_step": int(np.mean(n_traced)),
                           "surrogate_rel_err": _quantiles(es), "output_rel_err": _quantiles(eo),

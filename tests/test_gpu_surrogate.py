@@ -278,3 +278,16 @@ def test_audit_flags_rule():
     assert np.array_equal(f, g)
     h = surrogate.audit_flags_host(spread, seed=5, fraction=0.02, threshold=1e-3)
     assert not np.array_equal(f & 1, h & 1)
+
+
+def test_fourier_scale_selection(small):
+    omega, s1, ah = surrogate.training_set(small, n=8192, seed=31)
+    x7 = surrogate.inputs(omega, s1, small.xray, small.omega_axis, small.F)
+    best, scores = surrogate.select_fourier_scale(x7, np.log(ah), candidates=(0.35, 0.5), steps=300,
+                                                  batch=1024, members=2, seed=5)
+    assert best in (0.35, 0.5) and set(scores) == {0.35, 0.5}
+    for fb, med in scores.values():
+        assert 0.0 <= fb <= 1.0 and np.isfinite(med) and med < 0.5
+    assert scores[best] == min(scores.values())
+    with pytest.raises(ValueError):
+        surrogate.select_fourier_scale(x7[:1], np.log(ah[:1]))

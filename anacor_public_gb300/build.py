@@ -26,7 +26,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-std=c++17", "-Wall"]
 
-CU_SOURCES = ["trace_kernels.cu", "voxel_order.cu", "noalloc.cu", "surrogate.cu", "gridding.cu", "sampling.cu"]
+CU_SOURCES = ["trace_kernels.cu", "voxel_order.cu", "noalloc.cu", "surrogate.cu", "gridding.cu", "sampling.cu",
+              "distance_field.cu"]
 CPP_SOURCES = ["reflection_setup.cpp", "capi.cpp", "gridding_capi.cpp"]
 
 

@@ -65,7 +65,7 @@ struct DeviceState {
     cudaStream_t stream = nullptr;
     double *qtab = nullptr;   // quotient table for den <= qtab_den (never freed: plans keep pointers)
     int qtab_den = 0;
-    int bps[5] = {0, 0, 0, 0, 0};   // CTAs per SM of each register-budget variant (index 1..4)
+    int bps[kVariants + 1] = {};    // CTAs per SM of each kernel variant (index 1..kVariants)
 };
 
 
@@ -224,6 +224,8 @@ struct anacor_plan {
     int variant = 0;               // register-budget variant (0: process default)
     int order = 1;                 // voxel order of the packed list (0 the caller's, 1 Morton, 2.. blocked)
     long long *d_c64 = nullptr;    // the caller's int64 voxel list (for re-packing)
+    uint8_t *d_field = nullptr;    // label | distance << 3, built on first use by variants 5..8
+    int field_state = 0;           // 0 not built, 1 built, -1 labels outside 0..7 (no field)
 };
 
 namespace {
@@ -243,6 +245,7 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_steps, st);
     dev_free(p->d_sq, st);
     dev_free(p->d_c64, st);
+    dev_free(p->d_field, st);
     if (p->h_refl)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
@@ -438,6 +441,39 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
     return plan_ensure_partial(p);
 }
 
+// The packed distance field of the plan's volume (variants 5..8), built once.
+int plan_ensure_field(anacor_plan *p)
+{
+    if (p->field_state == 1)
+        return kOk;
+    if (p->field_state < 0)
+        return fail(kErrUnsupported, "the distance-field march needs labels in 0..7");
+    cudaStream_t st = p->stream;
+    const size_t nvol = (size_t)p->dims[0] * p->dims[1] * p->dims[2];
+    uint8_t *tmp = nullptr;
+    int *d_bad = nullptr;
+    int bad = 0;
+    cudaError_t e;
+    if ((e = dev_alloc(&p->d_field, nvol, st)) || (e = dev_alloc(&tmp, nvol, st)) || (e = dev_alloc(&d_bad, 1, st)) ||
+        (e = launch_distance_field(p->d_vol, p->dims, p->d_field, tmp, d_bad, st)) ||
+        (e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st))) {
+        dev_free(tmp, st);
+        dev_free(d_bad, st);
+        dev_free(p->d_field, st);
+        return cuda_fail(e, "distance field");
+    }
+    dev_free(tmp, st);
+    dev_free(d_bad, st);
+    if (bad) {
+        dev_free(p->d_field, st);
+        p->field_state = -1;
+        return fail(kErrUnsupported, "the distance-field march needs labels in 0..7");
+    }
+    p->field_state = 1;
+    return kOk;
+}
+
 SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
 {
     SampleDesc d;
@@ -465,6 +501,7 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     d.sq_stride = p->sq_stride;
     d.qtab = p->d_qtab;
     d.work_begin = work_begin;
+    d.field = p->field_state == 1 ? p->d_field : nullptr;
     return d;
 }
 
@@ -552,6 +589,8 @@ int plan_launch_bisection(anacor_plan *p, cudaStream_t st, int num_cls)
     return kOk;
 }
 
+int plan_default_config(anacor_plan *p);
+
 int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, int64_t n, const double *voxel,
              const double *mu, int full, int is_exp, const double *s1, const double *omega, int64_t n_refl,
              const double *xray, const double *axis, const double *F, const ReflTable *tables, int threads,
@@ -561,6 +600,8 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
     if (!st)
         st = plan_reserve_refl(&p, n_refl);
+    if (!st && !ib_cls)
+        st = plan_default_config(&p);
     if (!st) {
         if (tables)
             std::memcpy(p.h_refl, tables, (size_t)n_refl * sizeof(ReflTable));
@@ -584,9 +625,12 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
 
 int plan_configure(anacor_plan *p, int variant, int tile, int order)
 {
-    if (variant < 0 || variant > 4 || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) || order < -1 ||
-        order >= kVoxelOrders)
+    if (variant < 0 || variant > kVariants || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) ||
+        order < -1 || order >= kVoxelOrders)
         return fail(kErrArgs, "bad plan configuration");
+    if (variant > 4)
+        if (int st = plan_ensure_field(p))
+            return st;
     cudaError_t e;
     if (order >= 0 && order != p->order && p->n_vox > 0) {
         e = launch_pack_coords_order(p->d_c64, p->n_vox, p->dims, order, p->d_coords, p->d_status, p->stream);
@@ -647,6 +691,52 @@ struct TuneVal {
     float ms;
 };
 std::map<TuneKey, TuneVal> g_tune_cache;
+
+TuneKey tune_key(const anacor_plan *p)
+{
+    int nb = 0;
+    while ((1 << nb) < p->n_vox)
+        nb++;
+    return TuneKey{p->dims[0], p->dims[1], p->dims[2], nb};
+}
+
+bool tune_lookup(const anacor_plan *p, TuneVal &v)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_tune_cache.find(tune_key(p));
+    if (it == g_tune_cache.end())
+        return false;
+    v = it->second;
+    return true;
+}
+
+// Configuration of a plan run without autotuning (the drop-in entry points):
+// the process's tuned choice for this volume class when there is one; else
+// the distance-field march for volumes with an axis of 256 voxels or more
+// (long legs: it steps over most increments; 20-40 % faster there, 20 %
+// slower on a 96^3 volume) and the cooperative march below that, with the
+// largest tile up to 1024 voxels that still gives every warp four work items.
+int plan_default_config(anacor_plan *p)
+{
+    TuneVal v{0, 0, 1, 0.0f};
+    if (tune_lookup(p, v) && (v.variant <= 4 || plan_ensure_field(p) == kOk))
+        return plan_configure(p, v.variant, v.tile, v.order);
+    int variant = 0;
+    const int big = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
+    if (!std::getenv("ANACOR_CTAS_PER_SM") && big >= 256) {
+        if (plan_ensure_field(p) == kOk)
+            variant = 8;
+        succeed();   // labels outside 0..7: the cooperative march, no error
+    }
+    const long long warps = (long long)p->dev->sms * 32;
+    int tile = kMinTile;
+    for (int t : {1024, 512, 256})
+        if (p->n_refl * (((long long)p->n_vox + t - 1) / t) >= 4 * warps) {
+            tile = t;
+            break;
+        }
+    return plan_configure(p, variant, tile, -1);
+}
 
 }  // namespace
 
@@ -926,6 +1016,41 @@ int anacor_plan_count_steps(anacor_plan *p, uint64_t *total)
     if (st)
         return st;
     *total = h;
+    return succeed();
+}
+
+int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *out)
+{
+    if (!label || !shape || !out)
+        return fail(kErrArgs, "null argument");
+    if (!valid_shape(shape))
+        return fail(kErrArgs, "volume axes must lie in [1, 8191] and the volume below 2^31 voxels");
+    DeviceState *dev = nullptr;
+    if (int st = current_device(&dev))
+        return st;
+    cudaStream_t st = dev->stream;
+    const int dims[3] = {(int)shape[0], (int)shape[1], (int)shape[2]};
+    const size_t nvol = (size_t)shape[0] * shape[1] * shape[2];
+    int8_t *d_vol = nullptr;
+    uint8_t *d_out = nullptr, *d_tmp = nullptr;
+    int *d_bad = nullptr;
+    int bad = 0;
+    cudaError_t e;
+    if (!(e = dev_alloc(&d_vol, nvol, st)) && !(e = dev_alloc(&d_out, nvol, st)) && !(e = dev_alloc(&d_tmp, nvol, st)) &&
+        !(e = dev_alloc(&d_bad, 1, st)) &&
+        !(e = cudaMemcpyAsync(d_vol, label, nvol, cudaMemcpyHostToDevice, st)) &&
+        !(e = launch_distance_field(d_vol, dims, d_out, d_tmp, d_bad, st)) &&
+        !(e = cudaMemcpyAsync(out, d_out, nvol, cudaMemcpyDeviceToHost, st)) &&
+        !(e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st)))
+        e = cudaStreamSynchronize(st);
+    dev_free(d_vol, st);
+    dev_free(d_out, st);
+    dev_free(d_tmp, st);
+    dev_free(d_bad, st);
+    if (e)
+        return cuda_fail(e, "distance field");
+    if (bad)
+        return fail(kErrUnsupported, "the distance field needs labels in 0..7");
     return succeed();
 }
 
@@ -1288,19 +1413,14 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
 {
     if (!p || p->n_refl <= 0 || p->n_vox <= 0)
         return fail(kErrArgs, "autotune needs a plan with voxels and reflections");
-    int nb = 0;
-    while ((1 << nb) < p->n_vox)
-        nb++;
-    const TuneKey key{p->dims[0], p->dims[1], p->dims[2], nb};
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) {
-            const TuneVal v = it->second;
-            if (best_ms)
-                *best_ms = v.ms;
-            return plan_configure(p, v.variant, v.tile, v.order) ? t_status : succeed();
-        }
+    const TuneKey key = tune_key(p);
+    TuneVal cv{0, 0, 1, 0.0f};
+    const bool cached = tune_lookup(p, cv);
+    // a cached distance-field choice does not apply to a volume without a field
+    if (cached && (cv.variant <= 4 || plan_ensure_field(p) == kOk)) {
+        if (best_ms)
+            *best_ms = cv.ms;
+        return plan_configure(p, cv.variant, cv.tile, cv.order) ? t_status : succeed();
     }
     // first the voxel order at the default variant and tile, then variant x tile with that order
     TuneVal best{0, 0, 1, 1e30f};
@@ -1341,8 +1461,12 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
             t_order = t;
         }
     }
+    // the distance-field variants where the labels allow a field
+    std::vector<int> variants{2, 3, 4};
+    if (plan_ensure_field(p) == kOk)
+        variants.insert(variants.end(), {6, 7, 8});
     for (int tile : {128, 256, 512, 1024, 2048})
-        for (int variant : {2, 3, 4}) {
+        for (int variant : variants) {
             float t = 0.0f;
             if (int st = timed(variant, tile, order, t))
                 return st;
@@ -1401,8 +1525,12 @@ anacor_batch *anacor_batch_create(anacor_plan *const *plans, int n_plans)
 
 int anacor_batch_configure(anacor_batch *b, int variant)
 {
-    if (!b || variant < 0 || variant > 4)
+    if (!b || variant < 0 || variant > kVariants)
         return fail(kErrArgs, "bad arguments");
+    if (variant > 4)
+        for (anacor_plan *p : b->plans)
+            if (int st = plan_ensure_field(p))
+                return st;
     b->variant = variant;
     if (int st = batch_upload(b))
         return st;
@@ -1480,10 +1608,16 @@ int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl)
                 return st;
     float best = 1e30f;
     int best_v = 0;
+    std::vector<int> variants{2, 3, 4};
+    bool fields = true;
+    for (anacor_plan *p : b->plans)
+        fields = fields && plan_ensure_field(p) == kOk;
+    if (fields)
+        variants.insert(variants.end(), {6, 7, 8});
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int v : {2, 3, 4}) {
+    for (int v : variants) {
         b->variant = v;
         if (int st = batch_upload(b))
             return st;

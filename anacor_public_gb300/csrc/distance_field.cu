@@ -1,0 +1,115 @@
+// Chessboard distance field of a label volume, packed with the label.
+//
+// out[v] = (label & 7) | (min(D(v), 31) << 3), where D(v) is the chessboard
+// (L-infinity) distance from voxel v to the nearest voxel of the volume whose
+// label differs from v's, and 0 for vacuum voxels (label 0: a ray stops there,
+// so their distance is never read).  Every voxel within chessboard distance
+// D(v) - 1 of v carries v's label: a march that stands on v may step over the
+// increments that provably stay inside that cube.
+//
+// D is found as the largest uniform cube around v, built from one axis at a
+// time (the cube of radius r is uniform iff every row segment of half-width r
+// inside it is):
+//   rows    d_x(v)   = min(31, distance to the nearest other label along x)
+//   planes  d_xy(v)  = 1 + max{ r : all |dy| <= r have v's label and d_x >= r + 1 }
+//   volume  D(v)     = 1 + max{ r : all |dz| <= r have v's label and d_xy >= r + 1 }
+// Voxels outside the volume do not count (marches never leave it).  The
+// labels must fit 3 bits (0..7); the first pass flags any that do not.
+#include "anacor_internal.h"
+#include "trace_launch.h"
+
+namespace anacor {
+namespace {
+
+constexpr int kFieldCap = 31;
+constexpr int kFieldThreads = 256;
+
+// d_x along each row; one CTA per (z, y) row
+__global__ void __launch_bounds__(kFieldThreads) field_rows(const int8_t *__restrict__ vol, int dx,
+                                                            uint8_t *__restrict__ out, int *__restrict__ bad)
+{
+    const long long row = (long long)blockIdx.x * dx;
+    const int8_t *r = vol + row;
+    bool any_bad = false;
+    for (int x0 = 0; x0 < dx; x0 += kFieldThreads) {
+        const int x = x0 + (int)threadIdx.x;
+        if (x < dx) {
+            const int lab = r[x];
+            uint8_t o = 0;
+            if ((unsigned)lab > 7u) {
+                any_bad = true;
+            } else if (lab != 0) {
+                int d = kFieldCap;
+                for (int k = 1; k < kFieldCap; k++) {
+                    if ((x + k < dx && r[x + k] != lab) || (x - k >= 0 && r[x - k] != lab)) {
+                        d = k;
+                        break;
+                    }
+                }
+                o = (uint8_t)(lab | (d << 3));
+            }
+            out[row + x] = o;
+        }
+    }
+    if (__syncthreads_or(any_bad) && threadIdx.x == 0)
+        atomicOr(bad, 1);
+}
+
+// One cube-growing pass along an axis of stride `stride` and extent `n`
+// (coordinate `c` of the row's voxels on that axis): in holds label | d << 3
+// of the previous pass, out receives label | d' << 3.
+__global__ void __launch_bounds__(kFieldThreads) field_grow(const uint8_t *__restrict__ in, int dy, int dx,
+                                                            int axis, int n, long long stride,
+                                                            uint8_t *__restrict__ out)
+{
+    const long long row = (long long)blockIdx.x * dx;
+    const int c = axis == 1 ? (int)(blockIdx.x % (unsigned)dy) : (int)(blockIdx.x / (unsigned)dy);
+    for (int x0 = 0; x0 < dx; x0 += kFieldThreads) {
+        const int x = x0 + (int)threadIdx.x;
+        if (x >= dx)
+            continue;
+        const long long v = row + x;
+        const uint32_t b = in[v];
+        const uint32_t lab = b & 7u;
+        if (lab == 0) {
+            out[v] = 0;
+            continue;
+        }
+        uint32_t m = b >> 3;
+        int d = 1;
+        for (int r = 1; r < kFieldCap; r++) {
+            if (c + r < n) {
+                const uint32_t u = in[v + r * stride];
+                m = min(m, (u & 7u) == lab ? (u >> 3) : 0u);
+            }
+            if (c - r >= 0) {
+                const uint32_t u = in[v - r * stride];
+                m = min(m, (u & 7u) == lab ? (u >> 3) : 0u);
+            }
+            if (m < (uint32_t)(r + 1))
+                break;
+            d = r + 1;
+        }
+        out[v] = (uint8_t)(lab | (uint32_t)d << 3);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_distance_field(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
+                                  cudaStream_t st)
+{
+    const unsigned rows = (unsigned)dims[0] * (unsigned)dims[1];
+    if (rows == 0 || dims[2] == 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+    if (e != cudaSuccess)
+        return e;
+    const long long plane = (long long)dims[1] * dims[2];
+    field_rows<<<rows, kFieldThreads, 0, st>>>(d_vol, dims[2], d_out, d_bad);
+    field_grow<<<rows, kFieldThreads, 0, st>>>(d_out, dims[1], dims[2], 1, dims[1], dims[2], d_tmp);
+    field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp, dims[1], dims[2], 0, dims[0], plane, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace anacor

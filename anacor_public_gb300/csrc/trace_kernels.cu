@@ -62,6 +62,7 @@ constexpr unsigned kAll = 0xffffffffu;
 struct Vol {
     const int8_t *p;
     int dz, dy, dx;
+    const uint8_t *field = nullptr;   // label | distance << 3, for the distance-field march
 };
 
 __device__ __forceinline__ int pick3(int k, int z, int y, int x)
@@ -313,9 +314,11 @@ __device__ __noinline__ void march_lane(const FaceRule &R, int cz, int cy, int c
     }
 }
 
-// Label of increment `inc` from the reference's FP64 expression (an
-// increment whose fixed-point fraction lies near a rounding boundary).
-__device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol v)
+// Byte of `bytes` (the label volume or its packed distance field) at
+// increment `inc`, from the reference's FP64 expression (an increment whose
+// fixed-point fraction lies near a rounding boundary).
+__device__ __noinline__ uint32_t exact_byte(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol v,
+                                            const uint8_t *bytes)
 {
     int pz, py, px;
     const int s = G.count_axis;
@@ -323,7 +326,12 @@ __device__ __noinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, 
     pz = s == 0 ? cz + inc * ds : exact_axis(cz, inc, G.q[0], G.use_round, v.dz);
     py = s == 1 ? cy + inc * ds : exact_axis(cy, inc, G.q[1], G.use_round, v.dy);
     px = s == 2 ? cx + inc * ds : exact_axis(cx, inc, G.q[2], G.use_round, v.dx);
-    return (uint32_t)__ldg(reinterpret_cast<const uint8_t *>(v.p) + (pz * v.dy + py) * v.dx + px);
+    return (uint32_t)__ldg(bytes + (pz * v.dy + py) * v.dx + px);
+}
+
+__device__ __forceinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol &v)
+{
+    return exact_byte(G, cz, cy, cx, inc, v, reinterpret_cast<const uint8_t *>(v.p));
 }
 
 // Increments i >= 0 for which c + i*q stays at least 2 voxels inside [0, h]
@@ -343,6 +351,60 @@ __device__ __forceinline__ int wall_increments(double q, int c, int h)
     if (!(k >= 0.0f))
         return -1;
     return (int)fminf(floorf(k * 0.9999f), 1.0e9f);
+}
+
+// Distance-field march of one lane over increments 1 .. lim-1 (all clear of
+// the volume's walls, as for the cooperative march).  The field byte of the
+// current increment i gives the label and D, the chessboard distance to the
+// nearest voxel with another label.  Increment i + n lies n voxels away on
+// the step axis and at most ceil(n qmax) + 1 on the other two (two roundings
+// of c + n q), so every increment up to i + nmax(D) with
+//     nmax(D) = min(D - 1, floor((D - 2) / qmax))
+// carries increment i's label: it is accepted without a load, and the march
+// goes on at i + nmax + 1.  Labels, stops, class changes and len_path_2 are
+// therefore exactly those of the per-increment march.
+__device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx,
+                                            const Vol &v, int base, int lim, uint32_t b0, March &m, bool &stopped,
+                                            uint16_t *seg)
+{
+    // qmax rounded up and 2^16 / qmax rounded down: the skip never exceeds nmax
+    const float qm = fmaxf(__double2float_ru(fabs(R.q[g.ia])), __double2float_ru(fabs(R.q[g.ib])));
+    const uint32_t rq = qm < 0.015625f ? (1u << 22) : (uint32_t)__fdiv_rd(65536.0f, qm);
+    auto nmax = [rq](uint32_t d) -> int {
+        return d < 2u ? 0 : min((int)d - 1, (int)(((d - 2u) * rq) >> 16));
+    };
+    const uint8_t *pk = v.field + base;
+    int prev = m.prev, nseg = m.nseg;
+    int i = 1 + nmax(b0 >> 3);
+    int last = min(i - 1, lim - 1);
+    while (i < lim) {
+        const long long ea = g.off + (long long)i * g.Qa, eb = g.off + (long long)i * g.Qb;
+        uint32_t b;
+        if (((uint32_t)ea + g.Ma < 2u * g.Ma) | ((uint32_t)eb + g.Mb < 2u * g.Mb))
+            b = exact_byte(R, cz, cy, cx, i, v, v.field);
+        else
+            b = __ldg(pk + (i * g.ds * g.Ss + (int)(ea >> 32) * g.Sa + (int)(eb >> 32) * g.Sb));
+        const int lab = (int)(b & 7u);
+        if (lab == 0) {
+            stopped = true;
+            last = i - 1;
+            break;
+        }
+        if (lab != prev) {
+            if (lab <= 4) {
+                if (nseg < kMaxSegments)
+                    seg[nseg * kBlock] = (uint16_t)((lab << 13) | i);
+                nseg++;
+            }
+            prev = lab;
+        }
+        const int n = nmax(b >> 3);
+        last = min(i + n, lim - 1);
+        i += n + 1;
+    }
+    m.last_i = last;
+    m.prev = prev;
+    m.nseg = nseg;
 }
 
 struct LegResult {
@@ -377,7 +439,7 @@ __device__ __forceinline__ double sq_len(const double *sq, int stride, int axis,
 // kF32: the per-class lengths in FP32 (for A_h, which needs 1e-6; the march
 // itself, and hence the visited voxels, segments and len_path_2, is the same);
 // otherwise FP64 in the reference's order (bit-exact lengths).
-template <bool kDetail, bool kF32 = false>
+template <bool kDetail, bool kF32 = false, bool kField = false>
 __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
                                           bool valid, const Vol &v, int full, const double *voxel,
                                           const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
@@ -447,18 +509,30 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         if (coop) {
             base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
             seg[0] = (uint16_t)(3 << 13);
-            const int lab0 = __ldg(v.p + base);
-            if (lab0 == 0) {
-                stopped = true;
+            if (kField) {
+                // per lane, no warp synchronisation: the field march
+                const uint32_t b0 = __ldg(v.field + base);
+                if ((b0 & 7u) == 0) {
+                    stopped = true;
+                } else {
+                    m.prev = (int)(b0 & 7u);
+                    if (lim > 1)
+                        field_march(R, g, cz, cy, cx, v, base, lim, b0, m, stopped, seg);
+                }
             } else {
-                m.prev = lab0;
-                live = lim > 1;
+                const int lab0 = __ldg(v.p + base);
+                if (lab0 == 0) {
+                    stopped = true;
+                } else {
+                    m.prev = lab0;
+                    live = lim > 1;
+                }
             }
         }
     }
 
     // ---- cooperative march, one exit-face group at a time
-    unsigned pend = __ballot_sync(kAll, coop);
+    unsigned pend = kField ? 0u : __ballot_sync(kAll, coop);
     while (pend) {
         const int f = __shfl_sync(kAll, face, __ffs(pend) - 1);
         const unsigned grp = __ballot_sync(kAll, coop && face == f);
@@ -733,7 +807,7 @@ __device__ __forceinline__ void finish_item(float s, float c, const SampleDesc &
     }
 }
 
-template <int kMinBlocks>
+template <int kMinBlocks, bool kField>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const SampleDesc *__restrict__ descs,
                                                                         int n_desc, long long total_items,
                                                                         unsigned long long *__restrict__ work_counter)
@@ -765,7 +839,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         }
         __syncwarp();
 
-        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2]};
+        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field};
         float s = 0.0f, c = 0.0f;
         int bad = kOk;
         unsigned nsteps = 0;
@@ -780,7 +854,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
 #pragma unroll 1
             for (int leg = 0; leg < 2; leg++) {
                 LegResult a;
-                trace_leg<false, true>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v,
+                trace_leg<false, true, kField>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v,
                                        D.full_iteration, D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
                 bad |= a.status;
                 nsteps += valid ? (unsigned)a.len : 0u;
@@ -1235,12 +1309,18 @@ cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long t
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess)
         return e;
+#define ANACOR_LAUNCH(B, F) absorption_kernel<B, F><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter)
     switch (variant > 0 ? variant : absorption_variant()) {
-    case 1: absorption_kernel<1><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
-    case 3: absorption_kernel<3><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
-    case 4: absorption_kernel<4><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
-    default: absorption_kernel<2><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter); break;
+    case 1: ANACOR_LAUNCH(1, false); break;
+    case 3: ANACOR_LAUNCH(3, false); break;
+    case 4: ANACOR_LAUNCH(4, false); break;
+    case 5: ANACOR_LAUNCH(1, true); break;
+    case 6: ANACOR_LAUNCH(2, true); break;
+    case 7: ANACOR_LAUNCH(3, true); break;
+    case 8: ANACOR_LAUNCH(4, true); break;
+    default: ANACOR_LAUNCH(2, false); break;
     }
+#undef ANACOR_LAUNCH
     return cudaGetLastError();
 }
 
@@ -1300,12 +1380,18 @@ int absorption_block_threads() { return kBlock; }
 int absorption_occupancy(int *blocks_per_sm, int variant)
 {
     cudaError_t e;
+#define ANACOR_OCC(B, F) cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<B, F>, kBlock, 0)
     switch (variant > 0 ? variant : absorption_variant()) {
-    case 1: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<1>, kBlock, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<3>, kBlock, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<4>, kBlock, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<2>, kBlock, 0); break;
+    case 1: e = ANACOR_OCC(1, false); break;
+    case 3: e = ANACOR_OCC(3, false); break;
+    case 4: e = ANACOR_OCC(4, false); break;
+    case 5: e = ANACOR_OCC(1, true); break;
+    case 6: e = ANACOR_OCC(2, true); break;
+    case 7: e = ANACOR_OCC(3, true); break;
+    case 8: e = ANACOR_OCC(4, true); break;
+    default: e = ANACOR_OCC(2, false); break;
     }
+#undef ANACOR_OCC
     return e == cudaSuccess ? kOk : kErrCuda;
 }
 

@@ -42,6 +42,7 @@ struct SampleDesc {
     int sq_stride;
     const double *qtab;     // optional quotient table covering den <= max(dim)
     long long work_begin;   // first global work item of this sample
+    const uint8_t *field;   // label | distance << 3 (launch_distance_field); required by variants 5..8
 };
 
 // Absorption map of one sample (gridding mode): for every grid direction d and
@@ -90,7 +91,11 @@ int plan_view(const anacor_plan *p, PlanView *out);
 
 int rcp_table_init();
 int absorption_block_threads();
-// CTAs per SM of a register-budget variant (1..4; 0 = the process default)
+// Kernel variants: 1..4 the cooperative march with a register budget for
+// 1..4 CTAs per SM; 5..8 the same budgets with the distance-field march
+// (every sample needs its `field`).
+constexpr int kVariants = 8;
+// CTAs per SM of a variant (0 = the process default)
 int absorption_occupancy(int *blocks_per_sm, int variant = 0);
 // the process-default register-budget variant (CTAs per SM it targets)
 int absorption_variant();
@@ -116,6 +121,11 @@ cudaError_t unravel_voxels(const long long *d_lin, long long n_out, double step,
 // perm[k] = index in the caller's list of the k-th voxel of the packed list
 cudaError_t launch_order_permutation(const long long *d_c, int n, const int *dims, int order, int *d_perm,
                                      cudaStream_t st);
+// Chessboard distance field of a volume packed with its labels (see
+// distance_field.cu): d_out and d_tmp hold dims[0]*dims[1]*dims[2] bytes each;
+// *d_bad becomes nonzero when a label lies outside 0..7 (no field then).
+cudaError_t launch_distance_field(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
+                                  cudaStream_t st);
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs
 // take items from `d_counter` (reset inside the launch sequence).
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,

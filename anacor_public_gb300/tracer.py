@@ -268,3 +268,14 @@ def leg_detail(label, coords, s1_rot, xray_rot, voxel, full_iteration=0) -> dict
     _lib.check(st, L)
     return dict(face=face[:n], len=ln[:n], nseg=nseg[:n], first=first[:n], last=last[:n], L=Ls[:n],
                 status=status[:n])
+
+
+def distance_field(label) -> np.ndarray:
+    """The packed distance field that kernel variants 5..8 march on:
+    (label & 7) | (min(D, 31) << 3) per voxel, D the chessboard distance to the
+    nearest voxel with another label, 0 for label-0 voxels."""
+    L = _lib.load()
+    label = _c(label, np.int8)
+    out = np.zeros(label.shape, np.uint8)
+    _lib.check(L.anacor_distance_field(label, np.array(label.shape, dtype=np.int64), out), L)
+    return out

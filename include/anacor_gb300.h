@@ -141,13 +141,22 @@ int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *c
 
 /* Execution parameters of a plan (no counterpart in the reference; they do
  * not change the per-ray results, only the FP32 summation order of A_h):
- * variant = register-budget variant of the kernel, i.e. the CTAs per SM it is
- * compiled for (1..4, 0 = process default); tile = voxels per work item
+ * variant = kernel variant: 1..4 the warp-cooperative march compiled for
+ * 1..4 CTAs per SM, 5..8 the same register budgets with the distance-field
+ * march (steps over increments that a chessboard distance field proves to
+ * keep the label; needs labels in 0..7, else kErrUnsupported), 0 = process
+ * default; tile = voxels per work item
  * (>= 128, 0 = unchanged); order = voxel order of the packed list: 0 the
  * caller's, 1 Morton (Z-order) of (z, y, x), 2..7 blocked (Morton order of
  * blocks of 1x2x16, 1x4x8, 2x4x32, 4x8x64, 4x16x32 or 8x16x128 voxels, row
  * order inside a block), -1 unchanged. */
 int anacor_plan_configure(anacor_plan *p, int variant, int tile, int order);
+/* The packed distance field the variants 5..8 march on, for a host volume:
+ * out[v] = (label & 7) | (min(D, 31) << 3), D the chessboard distance from v
+ * to the nearest voxel of the volume with another label (0 for label-0
+ * voxels).  kErrUnsupported when a label lies outside 0..7.  No counterpart
+ * in the reference. */
+int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *out);
 int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *order);
 /* Autotuner: times every (variant, tile, order) candidate on the first
  * reflections of the plan (at least sample_refl of them) and keeps the

@@ -1,0 +1,179 @@
+"""Distance-field march (kernel variants 5..8).
+
+The packed field is checked against a CPU chessboard distance (min/max
+filters over growing cubes), and the march that steps over increments the
+field proves to keep their label against the oracle and against the
+per-increment cooperative march: the same len_path_2 totals, and A_h bit for
+bit under the same tile and voxel order (the per-voxel terms and their FP32
+summation order are the same).  A_h tolerance against the oracle: 1e-6
+relative, as for every other variant.
+"""
+import os
+
+import numpy as np
+import pytest
+from scipy import ndimage as nd
+
+from anacor_public_gb300 import _lib, build, synth, tracer
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-6
+K_UNSUPPORTED = 6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    build.build()
+
+
+def max_rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.abs(np.asarray(b))))
+
+
+def field_cpu(label):
+    """(label & 7) | (min(D, 31) << 3), D = 1 + the largest r whose clipped
+    cube around the voxel holds one label; 0 for label-0 voxels."""
+    lab = label.astype(np.int16)
+    D = np.ones(lab.shape, np.int32)
+    alive = np.ones(lab.shape, bool)
+    for r in range(1, 31):
+        # edge replication leaves the min and max of a clipped cube unchanged
+        mx = nd.maximum_filter(lab, size=2 * r + 1, mode="nearest")
+        mn = nd.minimum_filter(lab, size=2 * r + 1, mode="nearest")
+        alive &= (mx == lab) & (mn == lab)
+        if not alive.any():
+            break
+        D[alive] = r + 1
+    out = (lab & 7) | (D << 3)
+    out[lab == 0] = 0
+    return out.astype(np.uint8)
+
+
+def blocky_volume(shape, seed, n_boxes=40, labels=(1, 2, 3, 4, 5, 6, 7)):
+    rng = np.random.default_rng(seed)
+    vol = np.zeros(shape, np.int8)
+    for _ in range(n_boxes):
+        lo = [int(rng.integers(0, d)) for d in shape]
+        hi = [min(d, l + int(rng.integers(1, max(2, d // 2)))) for l, d in zip(lo, shape)]
+        vol[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] = rng.choice(labels)
+    return vol
+
+
+@pytest.mark.parametrize("shape,seed", [((20, 33, 47), 1), ((9, 70, 5), 2), ((64, 40, 72), 3), ((1, 1, 90), 4)])
+def test_field_matches_cpu(shape, seed):
+    vol = blocky_volume(shape, seed)
+    assert np.array_equal(tracer.distance_field(vol), field_cpu(vol))
+
+
+def test_field_of_a_sample_volume(small):
+    assert np.array_equal(tracer.distance_field(small.label), field_cpu(small.label))
+
+
+def test_field_caps_at_31():
+    vol = np.full((80, 70, 75), 3, np.int8)
+    vol[0, 0, 0] = 1
+    f = tracer.distance_field(vol)
+    assert (f >> 3).max() == 31 and f[40, 40, 40] == 3 | (31 << 3)
+    assert np.array_equal(f, field_cpu(vol))
+
+
+def test_field_rejects_labels_outside_0_to_7():
+    vol = np.ones((8, 9, 10), np.int8)
+    vol[3, 4, 5] = 9
+    with pytest.raises(_lib.AnacorError) as e:
+        tracer.distance_field(vol)
+    assert e.value.status == K_UNSUPPORTED
+    vol[3, 4, 5] = -1
+    with pytest.raises(_lib.AnacorError):
+        tracer.distance_field(vol)
+
+
+@pytest.fixture(scope="module")
+def sample():
+    return synth.small_sample(n_refl=48, seed=9)
+
+
+@pytest.fixture(scope="module")
+def want(sample, oracle):
+    return oracle.overall(sample, threads=os.cpu_count() or 1)
+
+
+@pytest.mark.parametrize("variant", [5, 6, 7, 8])
+@pytest.mark.parametrize("tile,order", [(512, 1), (2048, 0), (128, 3)])
+def test_field_variants_match_the_oracle_and_the_cooperative_march(sample, want, variant, tile, order):
+    p = tracer.Plan.from_sample(sample)
+    p.configure(variant, tile, order)
+    assert p.config() == {"variant": variant, "tile": tile, "order": order}
+    p.run()
+    a = p.result()
+    assert max_rel(a, want) <= RTOL
+    steps = p.count_steps()
+    p.configure(variant - 4, tile, order)
+    p.run()
+    assert np.array_equal(p.result(), a)
+    assert p.count_steps() == steps
+    p.close()
+
+
+def test_field_march_beamline_vs_golden(golden_dir):
+    gold = np.load(os.path.join(golden_dir, "beamline_ah.npz"))["ah"]
+    b = synth.beamline_sample(n_refl=12)
+    p = tracer.Plan.from_sample(b)
+    p.configure(8, 1024, 1)
+    p.run()
+    a = p.result()
+    assert max_rel(a, gold) <= RTOL
+    s8 = p.count_steps()
+    p.configure(4, 1024, 1)
+    p.run()
+    assert np.array_equal(p.result(), a)
+    assert p.count_steps() == s8
+    p.close()
+
+
+def _run(t, variant):
+    p = tracer.Plan.from_sample(t)
+    p.configure(variant, 512, 1)
+    p.run()
+    r = p.result()
+    n = p.count_steps()
+    p.close()
+    return r, n
+
+
+def test_field_march_on_wall_and_slab_volumes(oracle):
+    s = synth.small_sample(n_refl=24)
+    vols = []
+    v = np.full((20, 24, 28), 1, dtype=np.int8)   # crystal and liquor up to the walls: per-lane legs
+    v[4:16, 6:18, 2:26] = 3
+    vols.append(v)
+    v = np.ones((48, 56, 64), dtype=np.int8)      # more than 16 class changes per leg
+    for z in range(48):
+        v[z, :, :] = (1, 2, 4, 1, 2)[z % 5]
+    v[20:28, 24:32, 28:36] = 3
+    vols.append(v)
+    v = blocky_volume((40, 44, 48), 7, labels=(1, 2, 4, 5, 6))   # codes 5..7 change no class
+    v[14:26, 16:28, 18:30] = 3
+    vols.append(v)
+    for vol in vols:
+        coords = np.ascontiguousarray(np.argwhere(vol == 3).astype(np.int64))
+        t = synth.Sample(label=vol, coords=coords, s1=s.s1, omega=s.omega, xray=s.xray, omega_axis=s.omega_axis,
+                         F=s.F, voxel=s.voxel, mu=s.mu)
+        ref = oracle.overall(t, threads=4)
+        a8, n8 = _run(t, 8)
+        a4, n4 = _run(t, 4)
+        assert max_rel(a8, ref) <= RTOL
+        assert np.array_equal(a8, a4) and n8 == n4
+
+
+def test_field_variant_refused_for_wide_labels(sample):
+    vol = sample.label.copy()
+    vol[0, 0, 0] = 12
+    p = tracer.Plan(vol, sample.coords, sample.voxel, sample.mu)
+    p.set_reflections(sample.s1[:8], sample.omega[:8], sample.xray, sample.omega_axis, sample.F)
+    with pytest.raises(_lib.AnacorError) as e:
+        p.configure(8, 512, 1)
+    assert e.value.status == K_UNSUPPORTED
+    p.autotune()
+    assert p.config()["variant"] in (2, 3, 4)
+    p.close()

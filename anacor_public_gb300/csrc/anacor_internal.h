@@ -60,6 +60,9 @@ struct alignas(16) FaceRule {
     uint8_t count_kind;   // 0: c+1, 1: dim-c, 2: dim-c+1
     uint8_t vac_limit;    // consecutive-vacuum limit under full_iteration
     uint8_t pad;
+    // floor(2^16 / qmax) - 1 (at most 2^22), qmax the larger |q| of the two
+    // axes besides count_axis: the distance-field march's skip multiplier
+    uint32_t skip_rq;
 };
 static_assert(sizeof(FaceRule) == 64, "FaceRule layout");
 

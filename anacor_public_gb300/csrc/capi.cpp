@@ -482,9 +482,12 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     for (int a = 0; a < 3; a++) {
         d.dim[a] = p->dims[a];
         d.voxel[a] = p->voxel[a];
+        d.voxelf[a] = (float)p->voxel[a];
     }
-    for (int a = 0; a < 4; a++)
+    for (int a = 0; a < 4; a++) {
         d.mu[a] = p->mu[a];
+        d.muf[a] = (float)p->mu[a];
+    }
     d.n_vox = p->n_vox;
     d.coords = p->d_coords;
     d.refl = p->d_refl;

@@ -173,9 +173,12 @@ extern "C" int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *s
     for (int a = 0; a < 3; a++) {
         desc.dim[a] = dims[a];
         desc.voxel[a] = voxel[a];
+        desc.voxelf[a] = (float)voxel[a];
     }
-    for (int a = 0; a < 4; a++)
+    for (int a = 0; a < 4; a++) {
         desc.mu[a] = mu[a];
+        desc.muf[a] = (float)mu[a];
+    }
     desc.n_vox = (int)n_coords;
     desc.coords = d_pack;
     desc.refl = d_tables;

@@ -177,6 +177,15 @@ void face_rule(int face, double th, double ph, FaceRule &r)
             r.exact_mask |= uint8_t(1u << a);
     }
     r.fast = fast;
+    // never above 2^16 / qmax: the device's skip (D - 2) * skip_rq >> 16 stays
+    // within floor((D - 2) / qmax)
+    const double qmax = std::max(std::fabs(r.q[r.count_axis == 0 ? 1 : 0]), std::fabs(r.q[r.count_axis == 2 ? 1 : 2]));
+    if (!(qmax < kFastRatioLimit))
+        r.skip_rq = 0;
+    else if (qmax < 1.0 / 64.0)
+        r.skip_rq = 1u << 22;
+    else
+        r.skip_rq = (uint32_t)std::max(0.0, std::floor(65536.0 / qmax) - 1.0);
 }
 
 int fill_leg(const double *dir_my, bool incident, double th, double ph, LegHead &h, FaceRule *rules)

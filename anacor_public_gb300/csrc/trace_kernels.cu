@@ -72,7 +72,7 @@ __device__ __forceinline__ int pick3(int k, int z, int y, int x)
 
 // C's `int64_t n = floor(v)` / `round(v)`, then the reference's clamp.
 // Out-of-range and NaN conversions give INT64_MIN (x86-64 behaviour).
-__device__ __forceinline__ int exact_axis(int c, int i, double q, bool use_round, int dim)
+__device__ __noinline__ int exact_axis(int c, int i, double q, bool use_round, int dim)
 {
     const double v = __dadd_rn((double)c, __dmul_rn((double)i, q));
     const double r = use_round ? round(v) : floor(v);
@@ -93,15 +93,15 @@ __device__ __forceinline__ int exit_face(const LegHead &h, int cz, int cy, int c
 {
     // A zero distance (origin on a min plane, non-zero component) wins; ties
     // follow the reference's test order x_min, y_min, z_min.
-    if (cx == 0 && h.e[2] != 0.0) return 6;
-    if (cy == 0 && h.e[1] != 0.0) return 4;
-    if (cz == 0 && h.e[0] != 0.0) return 2;
     const uint32_t sb = h.sign_bits;
+    const bool hx = (sb & (4u | 32u)) != 0, hy = (sb & (2u | 16u)) != 0, hz = (sb & (1u | 8u)) != 0;
+    if (cx == 0 && hx) return 6;
+    if (cy == 0 && hy) return 4;
+    if (cz == 0 && hz) return 2;
     // one candidate per axis: numerator n_a
     const int nx = (sb & 4u) ? v.dx - cx : cx;
     const int ny = (sb & 2u) ? v.dy - cy : cy;
     const int nz = (sb & 1u) ? v.dz - cz : cz;
-    const bool hx = (sb & (4u | 32u)) != 0, hy = (sb & (2u | 16u)) != 0, hz = (sb & (1u | 8u)) != 0;
     const float inf = __int_as_float(0x7f800000);
     const float tx = hx ? (float)nx * h.inv[2] : inf;
     const float ty = hy ? (float)ny * h.inv[1] : inf;
@@ -233,7 +233,7 @@ __device__ __forceinline__ void leg_geom(const FaceRule &R, int cz, int cy, int 
     g.hb = pick3(b, v.dz, v.dy, v.dx) - 1;
     const int sz = v.dy * v.dx, sy = v.dx;
     g.Ss = pick3(s, sz, sy, 1); g.Sa = pick3(a, sz, sy, 1); g.Sb = pick3(b, sz, sy, 1);
-    g.ds = R.q[s] > 0.0 ? 1 : -1;
+    g.ds = R.Q[s] > 0 ? 1 : -1;   // the step axis's ratio is exactly +-1, so Q[s] = +-2^32
     g.Qa = R.Q[a]; g.Qb = R.Q[b];
     g.Ma = ((R.exact_mask >> a) & 1) ? 0u : kAmbiguityMargin;
     g.Mb = ((R.exact_mask >> b) & 1) ? 0u : kAmbiguityMargin;
@@ -367,9 +367,7 @@ __device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g,
                                             const Vol &v, int base, int lim, uint32_t b0, March &m, bool &stopped,
                                             uint16_t *seg)
 {
-    // qmax rounded up and 2^16 / qmax rounded down: the skip never exceeds nmax
-    const float qm = fmaxf(__double2float_ru(fabs(R.q[g.ia])), __double2float_ru(fabs(R.q[g.ib])));
-    const uint32_t rq = qm < 0.015625f ? (1u << 22) : (uint32_t)__fdiv_rd(65536.0f, qm);
+    const uint32_t rq = R.skip_rq;   // below 2^16 / qmax: the skip never exceeds nmax
     auto nmax = [rq](uint32_t d) -> int {
         return d < 2u ? 0 : min((int)d - 1, (int)(((d - 2u) * rq) >> 16));
     };
@@ -407,13 +405,6 @@ __device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g,
     m.nseg = nseg;
 }
 
-struct LegResult {
-    double L[4];       // FP64 lengths (kF32 == false)
-    float Lf[4];       // FP32 lengths (kF32 == true)
-    int face, len, nseg, status;
-    int first[3], last[3];
-};
-
 // fl(fl(d * v_axis)^2), from the sample's table when it has one
 __device__ __forceinline__ double sq_len(const double *sq, int stride, int axis, int d, double vox)
 {
@@ -422,6 +413,47 @@ __device__ __forceinline__ double sq_len(const double *sq, int stride, int axis,
     const double t = __dmul_rn((double)d, vox);
     return __dmul_rn(t, t);
 }
+
+struct L4 {
+    double v[4];
+};
+
+// cal_path2_plus by a second march, accumulating segments as they close (a
+// leg with more class changes than the shared buffer holds), out of line.
+__device__ __noinline__ L4 lengths_second_pass(const FaceRule &R, int cz, int cy, int cx, int steps, const Vol v,
+                                               int full, int len, int fz, int fy, int fx, int lz, int ly, int lx,
+                                               const double *voxel, const double *sq, int sq_stride,
+                                               const double *qtab, uint16_t *seg)
+{
+    const double yy = sq_len(sq, sq_stride, 1, abs(ly - fy), voxel[1]);
+    const double zz = sq_len(sq, sq_stride, 0, abs(lz - fz), voxel[0]);
+    const double xx = sq_len(sq, sq_stride, 2, abs(lx - fx), voxel[2]);
+    const double tot = __dsqrt_rn(__dadd_rn(__dadd_rn(yy, zz), xx));
+    const int den_i = len - 1;
+    const double2 dr = g_num_rcp[den_i];
+    March m2;
+    Sink s2;
+    s2.seg = seg;
+    s2.qtab = qtab;
+    s2.tot = tot; s2.den = dr.x; s2.rcp = dr.y; s2.den_i = den_i;
+    s2.L[0] = s2.L[1] = s2.L[2] = s2.L[3] = 0.0;
+    s2.open_cls = 3; s2.open_pos = 0; s2.seen = 0;
+    march_lane<1>(R, cz, cy, cx, steps, v, full, m2, s2);
+    const double q = seg_quotient(qtab, den_i, len - s2.open_pos, dr.x, dr.y);
+    add_class(s2.open_cls, __dmul_rn(tot, q), s2.seen, s2.L);
+    L4 r;
+    for (int k = 0; k < 4; k++)
+        r.v[k] = s2.L[k];
+    return r;
+}
+
+struct LegResult {
+    double L[4];       // FP64 lengths (kF32 == false)
+    float Lf[4];       // FP32 lengths (kF32 == true)
+    int face, len, nseg, status;
+    int first[3], last[3];
+};
+
 
 // cube_face + cal_coord + cal_path2_plus for one leg.  Called by all 32 lanes
 // of a warp together (warp-synchronous); `valid` marks lanes that hold a voxel.
@@ -443,7 +475,7 @@ template <bool kDetail, bool kF32 = false, bool kField = false>
 __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
                                           bool valid, const Vol &v, int full, const double *voxel,
                                           const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
-                                          LegResult &out)
+                                          LegResult &out, const float *voxelf = nullptr)
 {
     const int lane = threadIdx.x & 31;
     out.L[0] = out.L[1] = out.L[2] = out.L[3] = 0.0;
@@ -553,7 +585,7 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
                 // group constants, re-read from shared memory per chunk
                 const int gs = G.count_axis, ga = gs == 0 ? 1 : 0, gb = gs == 2 ? 1 : 2;
                 const int sz = v.dy * v.dx, sy = v.dx;
-                const int ds = G.q[gs] > 0.0 ? 1 : -1;
+                const int ds = G.Q[gs] > 0 ? 1 : -1;
                 const long long off = G.use_round ? 0x80000000ll : 0ll;
                 const uint32_t Ma = ((G.exact_mask >> ga) & 1) ? 0u : kAmbiguityMargin;
                 const uint32_t Mb = ((G.exact_mask >> gb) & 1) ? 0u : kAmbiguityMargin;
@@ -688,9 +720,12 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
     }
     if (kF32 && m.nseg <= kMaxSegments) {
         // total and segment fractions in FP32: tot * (span / (len - 1))
-        const float ty = __fmul_rn((float)abs(ly - fy), (float)voxel[1]);
-        const float tz = __fmul_rn((float)abs(lz - fz), (float)voxel[0]);
-        const float tx = __fmul_rn((float)abs(lx - fx), (float)voxel[2]);
+        const float vy = voxelf ? voxelf[1] : (float)voxel[1];
+        const float vz = voxelf ? voxelf[0] : (float)voxel[0];
+        const float vx = voxelf ? voxelf[2] : (float)voxel[2];
+        const float ty = __fmul_rn((float)abs(ly - fy), vy);
+        const float tz = __fmul_rn((float)abs(lz - fz), vz);
+        const float tx = __fmul_rn((float)abs(lx - fx), vx);
         const float totf = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ty, ty), __fmul_rn(tz, tz)), __fmul_rn(tx, tx)));
         const float scale = __fdiv_rn(totf, (float)(len - 1));
         int cur = seg[0];
@@ -706,6 +741,13 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
             out.Lf[3] += cls == 4 ? term : 0.0f;
             cur = nxt;
         }
+        return;
+    }
+    if (kF32) {
+        const L4 r = lengths_second_pass(R, cz, cy, cx, steps, v, full, len, fz, fy, fx, lz, ly, lx, voxel, sq,
+                                         sq_stride, qtab, seg);
+        for (int k = 0; k < 4; k++)
+            out.Lf[k] = (float)r.v[k];
         return;
     }
     // total from the first and last path points, y then z then x
@@ -843,7 +885,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         float s = 0.0f, c = 0.0f;
         int bad = kOk;
         unsigned nsteps = 0;
-        const float muf[4] = {(float)D.mu[0], (float)D.mu[1], (float)D.mu[2], (float)D.mu[3]};
         const int v0 = t * D.tile;
         const int v1 = min(D.n_vox, v0 + D.tile);
         // every lane runs the same number of iterations (the march is warp-synchronous)
@@ -855,7 +896,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             for (int leg = 0; leg < 2; leg++) {
                 LegResult a;
                 trace_leg<false, true, kField>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v,
-                                       D.full_iteration, D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
+                                       D.full_iteration, D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a,
+                                       D.voxelf);
                 bad |= a.status;
                 nsteps += valid ? (unsigned)a.len : 0u;
                 // the incident leg's lengths wait in shared memory while the
@@ -867,8 +909,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             }
             if (valid) {
                 // cal_rate's exponent (AnACor/src/ray_tracing_basic.c:1573-1576), in FP32
-                const float ex = muf[0] * lsum[0][tid] + muf[1] * lsum[1][tid] + muf[2] * lsum[2][tid] +
-                                 muf[3] * lsum[3][tid];
+                const float ex = D.muf[0] * lsum[0][tid] + D.muf[1] * lsum[1][tid] + D.muf[2] * lsum[2][tid] +
+                                 D.muf[3] * lsum[3][tid];
                 const float term = D.is_exp ? expf(-ex) : ex;
                 float ns, e;
                 two_sum(s, term, ns, e);

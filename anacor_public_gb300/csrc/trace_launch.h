@@ -33,6 +33,8 @@ struct SampleDesc {
     int is_exp;
     double mu[4];           // [liquor, loop, crystal, bubble]
     double voxel[3];        // z, y, x
+    float voxelf[3];        // (float) voxel, for the FP32 lengths of A_h
+    float muf[4];           // (float) mu, for the FP32 exponent of A_h
     double *out;            // [n_refl]
     double *partial;        // [n_refl * tiles] scratch
     unsigned int *arrive;   // [n_refl] scratch, zero before the first launch

@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--config", default=None,
+                    help="variant,tile,order for a single-sample plan instead of the autotuner (e.g. 8,1024,1)")
     ap.add_argument("--train-refl", type=int, default=100000, help="surrogate: traced training reflections")
     ap.add_argument("--train-steps", type=int, default=20000, help="surrogate: Adam steps")
     ap.add_argument("--train-batch", type=int, default=4096)
@@ -326,7 +328,9 @@ def run_ours(args):
         tuned = {"variant": info["variant"], "tiles": [p.config()["tile"] for p in plans],
                  "order": [p.config()["order"] for p in plans], "cuda_graph": True}
     else:
-        if not args.no_autotune:
+        if args.config:
+            plans[0].configure(*(int(x) for x in args.config.split(",")))
+        elif not args.no_autotune:
             plans[0].autotune()
         tuned = plans[0].config()
         grid, kernels = plans[0].launch_info()

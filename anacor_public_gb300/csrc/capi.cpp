@@ -747,11 +747,19 @@ int plan_default_config(anacor_plan *p)
 // from a captured CUDA graph.
 struct anacor_batch {
     std::vector<anacor_plan *> plans;
-    SampleDesc *d_descs = nullptr;
+    SampleDesc *d_descs = nullptr;        // every sample; the cooperative group first
     unsigned long long *d_counter = nullptr;
     long long items = 0;
     int variant = 0;
     int grid = 0;
+    // With a distance-field variant (5..8) the samples whose own plan marches
+    // on its field run in a second launch (d_descs_field, numbered from 0)
+    // and the others in a first, cooperative one with the same register budget.
+    SampleDesc *d_descs_field = nullptr;
+    unsigned long long *d_counter_field = nullptr;
+    int n_coop = 0, n_field = 0;
+    long long items_coop = 0, items_field = 0;
+    int grid_coop = 0, grid_field = 0;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -761,17 +769,39 @@ namespace {
 
 int batch_upload(anacor_batch *b)
 {
-    std::vector<SampleDesc> descs;
-    long long total = 0;
-    for (anacor_plan *p : b->plans) {
+    std::vector<anacor_plan *> coop, field;
+    for (anacor_plan *p : b->plans)
+        (b->variant > 4 && p->variant > 4 && p->field_state == 1 ? field : coop).push_back(p);
+    std::vector<SampleDesc> descs, descs_field;
+    long long total = 0, items_coop = 0;
+    for (anacor_plan *p : coop) {
         descs.push_back(plan_desc(p, total));
         total += (long long)p->n_refl * p->tiles;
     }
+    items_coop = total;
+    long long rebased = 0;
+    for (anacor_plan *p : field) {
+        descs.push_back(plan_desc(p, total));
+        descs_field.push_back(plan_desc(p, rebased));
+        const long long n = (long long)p->n_refl * p->tiles;
+        total += n;
+        rebased += n;
+    }
+    DeviceState *dev = b->plans[0]->dev;
     b->items = total;
-    b->grid = total ? grid_for(b->plans[0]->dev, b->variant, total) : 0;
+    b->grid = total ? grid_for(dev, b->variant, total) : 0;
+    b->n_coop = (int)coop.size();
+    b->n_field = (int)field.size();
+    b->items_coop = items_coop;
+    b->items_field = rebased;
+    b->grid_coop = items_coop ? grid_for(dev, b->variant > 4 ? b->variant - 4 : b->variant, items_coop) : 0;
+    b->grid_field = rebased ? grid_for(dev, b->variant, rebased) : 0;
     cudaError_t e;
     if ((e = cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice,
                              b->stream)) ||
+        (!descs_field.empty() &&
+         (e = cudaMemcpyAsync(b->d_descs_field, descs_field.data(), sizeof(SampleDesc) * descs_field.size(),
+                              cudaMemcpyHostToDevice, b->stream))) ||
         (e = cudaStreamSynchronize(b->stream)))
         return cuda_fail(e, "descriptor upload");
     // a captured graph holds the old grid: drop it
@@ -784,6 +814,33 @@ int batch_upload(anacor_batch *b)
         b->graph = nullptr;
     }
     return kOk;
+}
+
+// The batch's kernel launches on `st`: one over every sample, or (a
+// distance-field variant) the cooperative group then the field group.
+cudaError_t batch_enqueue(anacor_batch *b, cudaStream_t st)
+{
+    if (b->items <= 0)
+        return cudaSuccess;
+    if (b->variant <= 4 || b->n_field == 0)
+        return launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st,
+                                 b->variant > 4 ? b->variant - 4 : b->variant);
+    cudaError_t e = cudaSuccess;
+    if (b->items_coop > 0)
+        e = launch_absorption(b->d_descs, b->n_coop, b->items_coop, b->d_counter, b->grid_coop, st, b->variant - 4);
+    if (e == cudaSuccess && b->items_field > 0)
+        e = launch_absorption(b->d_descs_field, b->n_field, b->items_field, b->d_counter_field, b->grid_field, st,
+                              b->variant);
+    return e;
+}
+
+int batch_kernels(const anacor_batch *b)
+{
+    if (b->items <= 0)
+        return 0;
+    if (b->variant <= 4 || b->n_field == 0)
+        return 1;
+    return (b->items_coop > 0) + (b->items_field > 0);
 }
 
 int batch_check(anacor_batch *b, cudaStream_t st)
@@ -1108,8 +1165,13 @@ int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream)
     if ((e = cudaMemcpyAsync(d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice, st)))
         return cuda_fail(e, "descriptor upload");
     if (total > 0) {
-        const int grid = plan_grid(p0, total);
-        if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st, p0->variant)))
+        // one launch: the field march only when every sample has its field
+        int variant = p0->variant;
+        for (int i = 0; i < n_plans && variant > 4; i++)
+            if (plans[i]->field_state != 1)
+                variant -= 4;
+        const int grid = grid_for(p0->dev, variant, total);
+        if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st, variant)))
             return cuda_fail(e, "kernel launch");
     }
     if ((e = cudaStreamSynchronize(st)))
@@ -1509,7 +1571,9 @@ anacor_batch *anacor_batch_create(anacor_plan *const *plans, int n_plans)
     b->stream = plans[0]->stream;
     cudaError_t e;
     if ((e = cudaMalloc(&b->d_descs, sizeof(SampleDesc) * (size_t)n_plans)) ||
-        (e = cudaMalloc(&b->d_counter, sizeof(unsigned long long)))) {
+        (e = cudaMalloc(&b->d_counter, sizeof(unsigned long long))) ||
+        (e = cudaMalloc(&b->d_descs_field, sizeof(SampleDesc) * (size_t)n_plans)) ||
+        (e = cudaMalloc(&b->d_counter_field, sizeof(unsigned long long)))) {
         cuda_fail(e, "device allocation");
         anacor_batch_destroy(b);
         return nullptr;
@@ -1530,10 +1594,6 @@ int anacor_batch_configure(anacor_batch *b, int variant)
 {
     if (!b || variant < 0 || variant > kVariants)
         return fail(kErrArgs, "bad arguments");
-    if (variant > 4)
-        for (anacor_plan *p : b->plans)
-            if (int st = plan_ensure_field(p))
-                return st;
     b->variant = variant;
     if (int st = batch_upload(b))
         return st;
@@ -1545,12 +1605,8 @@ int anacor_batch_launch(anacor_batch *b, void *stream)
     if (!b)
         return fail(kErrArgs, "null batch");
     cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-    if (b->items > 0) {
-        cudaError_t e = launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st,
-                                          b->variant);
-        if (e)
-            return cuda_fail(e, "kernel launch");
-    }
+    if (cudaError_t e = batch_enqueue(b, st))
+        return cuda_fail(e, "kernel launch");
     return succeed();
 }
 
@@ -1570,9 +1626,7 @@ int anacor_batch_capture(anacor_batch *b, void *stream)
     cudaError_t e;
     if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)))
         return cuda_fail(e, "cudaStreamBeginCapture");
-    cudaError_t le = cudaSuccess;
-    if (b->items > 0)
-        le = launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st, b->variant);
+    const cudaError_t le = batch_enqueue(b, st);
     e = cudaStreamEndCapture(st, &b->graph);
     if (le)
         return cuda_fail(le, "kernel launch during capture");
@@ -1648,6 +1702,11 @@ int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl)
     return succeed();
 }
 
+int anacor_batch_kernels(const anacor_batch *b)
+{
+    return b ? batch_kernels(b) : 0;
+}
+
 int anacor_batch_info(const anacor_batch *b, int *grid, long long *items, int *variant)
 {
     if (!b)
@@ -1673,6 +1732,10 @@ void anacor_batch_destroy(anacor_batch *b)
         cudaFree(b->d_descs);
     if (b->d_counter)
         cudaFree(b->d_counter);
+    if (b->d_descs_field)
+        cudaFree(b->d_descs_field);
+    if (b->d_counter_field)
+        cudaFree(b->d_counter_field);
     delete b;
 }
 

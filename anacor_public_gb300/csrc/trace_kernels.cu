@@ -869,6 +869,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             break;
         const int si = find_sample(descs, n_desc, item);
         const SampleDesc &D = descs[si];
+        if (kField && !D.field) {
+            // a field variant launched over a sample without its field: an
+            // error status, no reads
+            if (lane == 0)
+                atomicOr(D.status, 1 << kErrArgs);
+            continue;
+        }
         const long long local = item - D.work_begin;
         const long long r = local / D.tiles;
         const int t = (int)(local - r * D.tiles);

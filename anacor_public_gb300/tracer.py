@@ -205,7 +205,8 @@ class Batch:
     def info(self) -> dict:
         g, n, v = ct.c_int(), ct.c_longlong(), ct.c_int()
         _lib.check(self._L.anacor_batch_info(self._h, ct.byref(g), ct.byref(n), ct.byref(v)), self._L)
-        return {"grid": g.value, "items": n.value, "variant": v.value}
+        return {"grid": g.value, "items": n.value, "variant": v.value,
+                "kernels": int(self._L.anacor_batch_kernels(self._h))}
 
     def results(self, stream: int | None = None):
         return [p.result(stream) for p in self.plans]

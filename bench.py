@@ -324,8 +324,9 @@ def run_ours(args):
         batch.capture(sh)
         run = lambda: batch.replay(sh)  # noqa: E731
         info = batch.info()
-        grid, kernels = info["grid"], 1
-        tuned = {"variant": info["variant"], "tiles": [p.config()["tile"] for p in plans],
+        grid, kernels = info["grid"], info["kernels"]
+        tuned = {"variant": info["variant"], "kernels_per_run": info["kernels"],
+                 "plan_variants": [p.config()["variant"] for p in plans], "tiles": [p.config()["tile"] for p in plans],
                  "order": [p.config()["order"] for p in plans], "cuda_graph": True}
     else:
         if args.config:

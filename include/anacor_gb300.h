@@ -182,6 +182,11 @@ int anacor_batch_replay(anacor_batch *b, void *stream);
 /* synchronise `stream` and check every plan's device status word */
 int anacor_batch_wait(anacor_batch *b, void *stream);
 int anacor_batch_info(const anacor_batch *b, int *grid, long long *items, int *variant);
+/* Kernel launches per batch run: 1, or 2 under a distance-field variant
+ * (5..8) when the batch mixes samples that march on their field (their plan
+ * configured to a field variant, e.g. by the autotuner) with samples that do
+ * not: those run first in the cooperative kernel of the same register budget. */
+int anacor_batch_kernels(const anacor_batch *b);
 void anacor_batch_destroy(anacor_batch *b);
 
 /* ------------------------------------------------- no-allocation entry -- */

@@ -177,3 +177,40 @@ def test_field_variant_refused_for_wide_labels(sample):
     p.autotune()
     assert p.config()["variant"] in (2, 3, 4)
     p.close()
+
+
+def test_batch_splits_field_and_cooperative_samples(oracle):
+    import torch
+    samples = synth.batch_samples(n_samples=3, max_refl=16, dim_range=(64, 128))
+    wide = samples[2].label.copy()
+    wide[0, 0, 0] = 9   # no field for this one
+    samples[2] = synth.Sample(label=wide, coords=samples[2].coords, s1=samples[2].s1, omega=samples[2].omega,
+                              xray=samples[2].xray, omega_axis=samples[2].omega_axis, F=samples[2].F,
+                              voxel=samples[2].voxel, mu=samples[2].mu)
+    wants = [oracle.overall(s, threads=os.cpu_count() or 1) for s in samples]
+    plans = [tracer.Plan.from_sample(s) for s in samples]
+    plans[0].configure(8, 512, 1)
+    plans[1].configure(4, 512, 1)
+    plans[2].configure(4, 512, 1)
+    b = tracer.Batch(plans)
+    st = torch.cuda.Stream()
+    got = {}
+    for v, kernels in ((8, 2), (4, 1), (7, 2)):
+        b.configure(v)
+        assert b.info()["kernels"] == kernels
+        b.launch(st.cuda_stream)
+        b.wait(st.cuda_stream)
+        got[v] = b.results(st.cuda_stream)
+        for g, w in zip(got[v], wants):
+            assert max_rel(g, w) <= RTOL
+    for g8, g4 in zip(got[8], got[4]):
+        assert np.array_equal(g8, g4)
+    b.configure(8)
+    b.capture(st.cuda_stream)
+    b.replay(st.cuda_stream)
+    b.wait(st.cuda_stream)
+    for g, g8 in zip(b.results(st.cuda_stream), got[8]):
+        assert np.array_equal(g, g8)
+    b.close()
+    for p in plans:
+        p.close()

@@ -363,46 +363,93 @@ __device__ __forceinline__ int wall_increments(double q, int c, int h)
 // carries increment i's label: it is accepted without a load, and the march
 // goes on at i + nmax + 1.  Labels, stops, class changes and len_path_2 are
 // therefore exactly those of the per-increment march.
+// One lane's field march over one leg, as a chain of dependent loads.
+struct FieldChain {
+    const FaceRule *R;
+    const uint8_t *pk;        // field + the leg's start voxel
+    long long off, Qa, Qb;
+    uint32_t Ma, Mb, rq;
+    int dS, Sa, Sb;           // strides of the step axis (signed) and the two others
+    int i, lim, last, prev, nseg;
+    bool on;
+};
+
+__device__ __forceinline__ int field_nmax(uint32_t d, uint32_t rq)
+{
+    return d < 2u ? 0 : min((int)d - 1, (int)(((d - 2u) * rq) >> 16));
+}
+
+__device__ __forceinline__ void chain_init(FieldChain &c, const FaceRule &R, const LegGeom &g, const Vol &v, int base,
+                                           int lim, uint32_t b0, const March &m)
+{
+    c.R = &R;
+    c.pk = v.field + base;
+    c.off = g.off;
+    c.Qa = g.Qa;
+    c.Qb = g.Qb;
+    c.Ma = g.Ma;
+    c.Mb = g.Mb;
+    c.rq = R.skip_rq;   // below 2^16 / qmax: the skip never exceeds nmax
+    c.dS = g.ds * g.Ss;
+    c.Sa = g.Sa;
+    c.Sb = g.Sb;
+    c.lim = lim;
+    c.prev = m.prev;
+    c.nseg = m.nseg;
+    c.i = 1 + field_nmax(b0 >> 3, c.rq);
+    c.last = min(c.i - 1, lim - 1);
+    c.on = c.i < lim;
+}
+
+// field byte of the chain's current increment
+__device__ __forceinline__ uint32_t chain_load(const FieldChain &c, int cz, int cy, int cx, const Vol &v)
+{
+    const long long ea = c.off + (long long)c.i * c.Qa, eb = c.off + (long long)c.i * c.Qb;
+    if (((uint32_t)ea + c.Ma < 2u * c.Ma) | ((uint32_t)eb + c.Mb < 2u * c.Mb))
+        return exact_byte(*c.R, cz, cy, cx, c.i, v, v.field);
+    return __ldg(c.pk + (c.i * c.dS + (int)(ea >> 32) * c.Sa + (int)(eb >> 32) * c.Sb));
+}
+
+// the stop / class-change test of the current increment, then the skip
+__device__ __forceinline__ void chain_step(FieldChain &c, uint32_t b, uint16_t *seg, bool &stopped)
+{
+    const int lab = (int)(b & 7u);
+    if (lab == 0) {
+        stopped = true;
+        c.last = c.i - 1;
+        c.on = false;
+        return;
+    }
+    if (lab != c.prev) {
+        if (lab <= 4) {
+            if (c.nseg < kMaxSegments)
+                seg[c.nseg * kBlock] = (uint16_t)((lab << 13) | c.i);
+            c.nseg++;
+        }
+        c.prev = lab;
+    }
+    const int n = field_nmax(b >> 3, c.rq);
+    c.last = min(c.i + n, c.lim - 1);
+    c.i += n + 1;
+    c.on = c.i < c.lim;
+}
+
+__device__ __forceinline__ void chain_done(const FieldChain &c, March &m)
+{
+    m.last_i = c.last;
+    m.prev = c.prev;
+    m.nseg = c.nseg;
+}
+
 __device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx,
                                             const Vol &v, int base, int lim, uint32_t b0, March &m, bool &stopped,
                                             uint16_t *seg)
 {
-    const uint32_t rq = R.skip_rq;   // below 2^16 / qmax: the skip never exceeds nmax
-    auto nmax = [rq](uint32_t d) -> int {
-        return d < 2u ? 0 : min((int)d - 1, (int)(((d - 2u) * rq) >> 16));
-    };
-    const uint8_t *pk = v.field + base;
-    int prev = m.prev, nseg = m.nseg;
-    int i = 1 + nmax(b0 >> 3);
-    int last = min(i - 1, lim - 1);
-    while (i < lim) {
-        const long long ea = g.off + (long long)i * g.Qa, eb = g.off + (long long)i * g.Qb;
-        uint32_t b;
-        if (((uint32_t)ea + g.Ma < 2u * g.Ma) | ((uint32_t)eb + g.Mb < 2u * g.Mb))
-            b = exact_byte(R, cz, cy, cx, i, v, v.field);
-        else
-            b = __ldg(pk + (i * g.ds * g.Ss + (int)(ea >> 32) * g.Sa + (int)(eb >> 32) * g.Sb));
-        const int lab = (int)(b & 7u);
-        if (lab == 0) {
-            stopped = true;
-            last = i - 1;
-            break;
-        }
-        if (lab != prev) {
-            if (lab <= 4) {
-                if (nseg < kMaxSegments)
-                    seg[nseg * kBlock] = (uint16_t)((lab << 13) | i);
-                nseg++;
-            }
-            prev = lab;
-        }
-        const int n = nmax(b >> 3);
-        last = min(i + n, lim - 1);
-        i += n + 1;
-    }
-    m.last_i = last;
-    m.prev = prev;
-    m.nseg = nseg;
+    FieldChain c;
+    chain_init(c, R, g, v, base, lim, b0, m);
+    while (c.on)
+        chain_step(c, chain_load(c, cz, cy, cx, v), seg, stopped);
+    chain_done(c, m);
 }
 
 // fl(fl(d * v_axis)^2), from the sample's table when it has one
@@ -455,29 +502,20 @@ struct LegResult {
 };
 
 
-// cube_face + cal_coord + cal_path2_plus for one leg.  Called by all 32 lanes
-// of a warp together (warp-synchronous); `valid` marks lanes that hold a voxel.
-//
-// Warp-cooperative march: lanes whose rays leave through the same face share
-// that face's step rule, and their 32.32 positions differ only in the integer
-// part (c * 2^32).  So the displacement of increment i -- and whether its
-// fraction is near a rounding boundary -- is the same for every lane of the
-// group: lane j computes it for increment i0 + j, the warp broadcasts it with
-// shuffles, and each lane only adds it to its own start address, loads the
-// label and checks it.  A lane joins the group only if no clamp can occur on
-// its increments (both end points at least one voxel inside the volume) and
-// the face has fixed-point ratios; other lanes, and full_iteration, use the
-// per-lane march.
-// kF32: the per-class lengths in FP32 (for A_h, which needs 1e-6; the march
-// itself, and hence the visited voxels, segments and len_path_2, is the same);
-// otherwise FP64 in the reference's order (bit-exact lengths).
-template <bool kDetail, bool kF32 = false, bool kField = false>
-__device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
-                                          bool valid, const Vol &v, int full, const double *voxel,
-                                          const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
-                                          LegResult &out, const float *voxelf = nullptr)
+// State of one leg between its set-up, its march and its lengths.
+struct LegState {
+    March m;
+    int face, lim, base;
+    bool need, coop, stopped, live;
+    uint32_t b0;   // field byte of increment 0 (field march)
+};
+
+// cube_face and the march set-up of one leg (warp-synchronous).  With kField
+// the field march runs here when kMarchNow, else the caller runs it.
+template <bool kDetail, bool kField, bool kMarchNow>
+__device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx, bool valid,
+                                          const Vol &v, int full, uint16_t *seg, LegResult &out, LegState &S)
 {
-    const int lane = threadIdx.x & 31;
     out.L[0] = out.L[1] = out.L[2] = out.L[3] = 0.0;
     out.Lf[0] = out.Lf[1] = out.Lf[2] = out.Lf[3] = 0.0f;
     out.len = 1; out.nseg = 1; out.status = kOk;
@@ -498,13 +536,12 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
     }
     March m;
     m.last_i = 0; m.nseg = 1; m.vac = 0; m.prev = 0;
-    Sink sk;
-    sk.seg = seg;
 
     // ---- set-up: step count, cooperative eligibility, increment 0.  Only a
     // few values cross the cooperative loop; the geometry is recomputed after.
     bool coop = false, stopped = false, live = false;
     int lim = 0, base = 0;
+    uint32_t b0 = 0;
     if (need) {
         const FaceRule &R = rules[face - 1];
         LegGeom g;
@@ -542,13 +579,15 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
             base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
             seg[0] = (uint16_t)(3 << 13);
             if (kField) {
-                // per lane, no warp synchronisation: the field march
-                const uint32_t b0 = __ldg(v.field + base);
+                // per lane, no warp synchronisation: the field march (now, or
+                // by the caller together with the other leg)
+                b0 = __ldg(v.field + base);
                 if ((b0 & 7u) == 0) {
                     stopped = true;
                 } else {
                     m.prev = (int)(b0 & 7u);
-                    if (lim > 1)
+                    live = lim > 1;
+                    if (kMarchNow && live)
                         field_march(R, g, cz, cy, cx, v, base, lim, b0, m, stopped, seg);
                 }
             } else {
@@ -563,8 +602,28 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
         }
     }
 
+    S.m = m;
+    S.face = face;
+    S.lim = lim;
+    S.base = base;
+    S.need = need;
+    S.coop = coop;
+    S.stopped = stopped;
+    S.live = live;
+    S.b0 = b0;
+}
+
+// The warp-cooperative march of the legs set up by leg_setup<.., false, ..>.
+__device__ __forceinline__ void leg_coop(const FaceRule *rules, int cz, int cy, int cx, const Vol &v, uint16_t *seg,
+                                         LegState &S)
+{
+    const int lane = threadIdx.x & 31;
+    const int face = S.face, lim = S.lim, base = S.base;
+    const bool coop = S.coop, live = S.live;
+    bool stopped = S.stopped;
+    March m = S.m;
     // ---- cooperative march, one exit-face group at a time
-    unsigned pend = kField ? 0u : __ballot_sync(kAll, coop);
+    unsigned pend = __ballot_sync(kAll, coop);
     while (pend) {
         const int f = __shfl_sync(kAll, face, __ffs(pend) - 1);
         const unsigned grp = __ballot_sync(kAll, coop && face == f);
@@ -666,6 +725,21 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
             }
         }
     }
+    S.m = m;
+    S.stopped = stopped;
+}
+
+// After the march: the per-lane remainder of the path and cal_path2_plus.
+template <bool kDetail, bool kF32>
+__device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy, int cx, const Vol &v, int full,
+                                           const double *voxel, const double *sq, int sq_stride, const double *qtab,
+                                           uint16_t *seg, LegState &S, LegResult &out, const float *voxelf)
+{
+    const int face = S.face, lim = S.lim;
+    const bool need = S.need, coop = S.coop, stopped = S.stopped;
+    March m = S.m;
+    Sink sk;
+    sk.seg = seg;
     if (!need)
         return;
 
@@ -786,6 +860,35 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
             out.Lf[k] = (float)s2.L[k];
         }
     }
+}
+
+// cube_face + cal_coord + cal_path2_plus for one leg.  Called by all 32 lanes
+// of a warp together (warp-synchronous); `valid` marks lanes that hold a voxel.
+//
+// Warp-cooperative march: lanes whose rays leave through the same face share
+// that face's step rule, and their 32.32 positions differ only in the integer
+// part (c * 2^32).  So the displacement of increment i -- and whether its
+// fraction is near a rounding boundary -- is the same for every lane of the
+// group: lane j computes it for increment i0 + j, the warp broadcasts it with
+// shuffles, and each lane only adds it to its own start address, loads the
+// label and checks it.  A lane joins the group only if no clamp can occur on
+// its increments (both end points at least one voxel inside the volume) and
+// the face has fixed-point ratios; other lanes, and full_iteration, use the
+// per-lane march.
+// kF32: the per-class lengths in FP32 (for A_h, which needs 1e-6; the march
+// itself, and hence the visited voxels, segments and len_path_2, is the same);
+// otherwise FP64 in the reference's order (bit-exact lengths).
+template <bool kDetail, bool kF32 = false, bool kField = false>
+__device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
+                                          bool valid, const Vol &v, int full, const double *voxel,
+                                          const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
+                                          LegResult &out, const float *voxelf = nullptr)
+{
+    LegState S;
+    leg_setup<kDetail, kField, true>(h, rules, cz, cy, cx, valid, v, full, seg, out, S);
+    if (!kField)
+        leg_coop(rules, cz, cy, cx, v, seg, S);
+    leg_finish<kDetail, kF32>(rules, cz, cy, cx, v, full, voxel, sq, sq_stride, qtab, seg, S, out, voxelf);
 }
 
 __device__ __forceinline__ int find_sample(const SampleDesc *d, int n, long long item)

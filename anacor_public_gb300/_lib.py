@@ -43,7 +43,7 @@ EXPORTS = (
     "ray_tracing_single_gridding", "ib_single_gridding", "nearest_neighbor_interpolate_overall",
     "anacor_plan_create_sampled", "anacor_plan_n_voxels", "anacor_plan_voxels", "anacor_sample_voxels",
     "anacor_plan_run_bisection", "anacor_bisection", "anacor_gridding_prepare", "anacor_gridding_run",
-    "anacor_distance_field", "anacor_batch_kernels",
+    "anacor_distance_field", "anacor_batch_kernels", "anacor_octant_fields",
 )
 
 _LIB = None
@@ -140,6 +140,8 @@ def load(path: str | None = None) -> ct.CDLL:
     L.anacor_plan_configure.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int]
     L.anacor_batch_kernels.restype = ct.c_int
     L.anacor_batch_kernels.argtypes = [ct.c_void_p]
+    L.anacor_octant_fields.restype = ct.c_int
+    L.anacor_octant_fields.argtypes = [_i8p, _i64p, np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")]
     L.anacor_distance_field.restype = ct.c_int
     L.anacor_distance_field.argtypes = [_i8p, _i64p, np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")]
     L.anacor_plan_config.restype = ct.c_int

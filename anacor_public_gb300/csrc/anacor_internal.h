@@ -59,7 +59,7 @@ struct alignas(16) FaceRule {
     uint8_t count_axis;   // axis whose coordinate sets the step count
     uint8_t count_kind;   // 0: c+1, 1: dim-c, 2: dim-c+1
     uint8_t vac_limit;    // consecutive-vacuum limit under full_iteration
-    uint8_t pad;
+    uint8_t octant;       // (dx < 0) | (dy < 0) << 1 | (dz < 0) << 2 of the march direction
     // floor(2^16 / qmax) - 1 (at most 2^22), qmax the larger |q| of the two
     // axes besides count_axis: the distance-field march's skip multiplier
     uint32_t skip_rq;

@@ -72,10 +72,16 @@ struct DeviceState {
 std::mutex g_mu;
 DeviceState g_dev[64];
 
+// Plan-level variants: 1..4 cooperative march, 5..8 the centred distance
+// field, 9..12 the octant fields; 9..12 run the kernels of 5..8.
+constexpr int kPlanVariants = 12;
+int kernel_variant(int v) { return v > kVariants ? v - 4 : v; }
+int budget_of(int v) { return v > 0 ? (v - 1) % 4 + 1 : absorption_variant(); }
+
 // CTAs per SM of `variant` (0: the process default) on this device
 int variant_occupancy(DeviceState *d, int variant)
 {
-    const int v = variant > 0 ? variant : absorption_variant();
+    const int v = variant > 0 ? kernel_variant(variant) : absorption_variant();
     std::lock_guard<std::mutex> lk(g_mu);
     if (!d->bps[v]) {
         int b = 0;
@@ -226,6 +232,8 @@ struct anacor_plan {
     long long *d_c64 = nullptr;    // the caller's int64 voxel list (for re-packing)
     uint8_t *d_field = nullptr;    // label | distance << 3, built on first use by variants 5..8
     int field_state = 0;           // 0 not built, 1 built, -1 labels outside 0..7 (no field)
+    uint8_t *d_field8 = nullptr;   // the 8 octant fields, built on first use by variants 9..12
+    int field8_state = 0;
 };
 
 namespace {
@@ -246,6 +254,7 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_sq, st);
     dev_free(p->d_c64, st);
     dev_free(p->d_field, st);
+    dev_free(p->d_field8, st);
     if (p->h_refl)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
@@ -442,36 +451,49 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
 }
 
 // The packed distance field of the plan's volume (variants 5..8), built once.
-int plan_ensure_field(anacor_plan *p)
+// The packed distance field(s) of the plan's volume, built once: kind 1 the
+// centred field (variants 5..8), kind 2 the 8 octant fields (9..12).
+int plan_ensure_field(anacor_plan *p, int kind = 1)
 {
-    if (p->field_state == 1)
+    uint8_t *&field = kind == 2 ? p->d_field8 : p->d_field;
+    int &state = kind == 2 ? p->field8_state : p->field_state;
+    if (state == 1)
         return kOk;
-    if (p->field_state < 0)
+    if (state < 0 || p->field_state < 0 || p->field8_state < 0)
         return fail(kErrUnsupported, "the distance-field march needs labels in 0..7");
     cudaStream_t st = p->stream;
     const size_t nvol = (size_t)p->dims[0] * p->dims[1] * p->dims[2];
+    const size_t copies = kind == 2 ? 8 : 1, tmp_copies = kind == 2 ? 6 : 1;
     uint8_t *tmp = nullptr;
     int *d_bad = nullptr;
     int bad = 0;
     cudaError_t e;
-    if ((e = dev_alloc(&p->d_field, nvol, st)) || (e = dev_alloc(&tmp, nvol, st)) || (e = dev_alloc(&d_bad, 1, st)) ||
-        (e = launch_distance_field(p->d_vol, p->dims, p->d_field, tmp, d_bad, st)) ||
+    if ((e = dev_alloc(&field, nvol * copies, st)) || (e = dev_alloc(&tmp, nvol * tmp_copies, st)) ||
+        (e = dev_alloc(&d_bad, 1, st)) ||
+        (e = kind == 2 ? launch_octant_fields(p->d_vol, p->dims, field, tmp, d_bad, st)
+                       : launch_distance_field(p->d_vol, p->dims, field, tmp, d_bad, st)) ||
         (e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
         (e = cudaStreamSynchronize(st))) {
         dev_free(tmp, st);
         dev_free(d_bad, st);
-        dev_free(p->d_field, st);
+        dev_free(field, st);
         return cuda_fail(e, "distance field");
     }
     dev_free(tmp, st);
     dev_free(d_bad, st);
     if (bad) {
-        dev_free(p->d_field, st);
-        p->field_state = -1;
+        dev_free(field, st);
+        state = -1;
         return fail(kErrUnsupported, "the distance-field march needs labels in 0..7");
     }
-    p->field_state = 1;
+    state = 1;
     return kOk;
+}
+
+// whether the plan's configured variant marches on a field it has
+bool plan_marches_field(const anacor_plan *p)
+{
+    return p->variant > kVariants ? p->field8_state == 1 : (p->variant > 4 && p->field_state == 1);
 }
 
 SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
@@ -504,7 +526,13 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     d.sq_stride = p->sq_stride;
     d.qtab = p->d_qtab;
     d.work_begin = work_begin;
-    d.field = p->field_state == 1 ? p->d_field : nullptr;
+    if (p->variant > kVariants) {
+        d.field = p->field8_state == 1 ? p->d_field8 : nullptr;
+        d.field_stride = (long long)p->dims[0] * p->dims[1] * p->dims[2];
+    } else {
+        d.field = p->field_state == 1 ? p->d_field : nullptr;
+        d.field_stride = 0;
+    }
     return d;
 }
 
@@ -548,7 +576,8 @@ int plan_launch(anacor_plan *p, cudaStream_t st)
     const long long items = (long long)p->n_refl * p->tiles;
     if (items == 0)
         return kOk;
-    cudaError_t e = launch_absorption(p->d_desc, 1, items, p->d_counter, plan_grid(p, items), st, p->variant);
+    cudaError_t e = launch_absorption(p->d_desc, 1, items, p->d_counter, plan_grid(p, items), st,
+                                      kernel_variant(p->variant));
     if (e != cudaSuccess)
         return cuda_fail(e, "kernel launch");
     return kOk;
@@ -628,11 +657,11 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
 
 int plan_configure(anacor_plan *p, int variant, int tile, int order)
 {
-    if (variant < 0 || variant > kVariants || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) ||
+    if (variant < 0 || variant > kPlanVariants || (tile != 0 && (tile < kMinTile || tile > (1 << 22))) ||
         order < -1 || order >= kVoxelOrders)
         return fail(kErrArgs, "bad plan configuration");
     if (variant > 4)
-        if (int st = plan_ensure_field(p))
+        if (int st = plan_ensure_field(p, variant > kVariants ? 2 : 1))
             return st;
     cudaError_t e;
     if (order >= 0 && order != p->order && p->n_vox > 0) {
@@ -716,19 +745,24 @@ bool tune_lookup(const anacor_plan *p, TuneVal &v)
 // Configuration of a plan run without autotuning (the drop-in entry points):
 // the process's tuned choice for this volume class when there is one; else
 // the distance-field march for volumes with an axis of 256 voxels or more
-// (long legs: it steps over most increments; 20-40 % faster there, 20 %
-// slower on a 96^3 volume) and the cooperative march below that, with the
-// largest tile up to 1024 voxels that still gives every warp four work items.
+// (long legs: it steps over most increments; 25-50 % faster there, while the
+// cooperative march is as fast on a 96^3 volume) and the cooperative march
+// below that, with the largest tile up to 1024 voxels that still gives every
+// warp four work items.
 int plan_default_config(anacor_plan *p)
 {
     TuneVal v{0, 0, 1, 0.0f};
-    if (tune_lookup(p, v) && (v.variant <= 4 || plan_ensure_field(p) == kOk))
+    if (tune_lookup(p, v) && (v.variant <= 4 || plan_ensure_field(p, v.variant > kVariants ? 2 : 1) == kOk))
         return plan_configure(p, v.variant, v.tile, v.order);
     int variant = 0;
     const int big = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
     if (!std::getenv("ANACOR_CTAS_PER_SM") && big >= 256) {
-        if (plan_ensure_field(p) == kOk)
-            variant = 8;
+        // the octant fields take 5x longer to build than the centred one and
+        // march 15-25 % faster: worth it once the run covers twice the volume
+        const long long nvol = (long long)p->dims[0] * p->dims[1] * p->dims[2];
+        const int kind = p->n_refl * (long long)p->n_vox >= 2 * nvol ? 2 : 1;
+        if (plan_ensure_field(p, kind) == kOk)
+            variant = kind == 2 ? 12 : 8;
         succeed();   // labels outside 0..7: the cooperative march, no error
     }
     const long long warps = (long long)p->dev->sms * 32;
@@ -771,7 +805,7 @@ int batch_upload(anacor_batch *b)
 {
     std::vector<anacor_plan *> coop, field;
     for (anacor_plan *p : b->plans)
-        (b->variant > 4 && p->variant > 4 && p->field_state == 1 ? field : coop).push_back(p);
+        (b->variant > 4 && plan_marches_field(p) ? field : coop).push_back(p);
     std::vector<SampleDesc> descs, descs_field;
     long long total = 0, items_coop = 0;
     for (anacor_plan *p : coop) {
@@ -789,13 +823,14 @@ int batch_upload(anacor_batch *b)
     }
     DeviceState *dev = b->plans[0]->dev;
     b->items = total;
-    b->grid = total ? grid_for(dev, b->variant, total) : 0;
+    const int cv = b->variant > 4 ? budget_of(b->variant) : b->variant;   // cooperative kernel
+    b->grid = total ? grid_for(dev, cv, total) : 0;
     b->n_coop = (int)coop.size();
     b->n_field = (int)field.size();
     b->items_coop = items_coop;
     b->items_field = rebased;
-    b->grid_coop = items_coop ? grid_for(dev, b->variant > 4 ? b->variant - 4 : b->variant, items_coop) : 0;
-    b->grid_field = rebased ? grid_for(dev, b->variant, rebased) : 0;
+    b->grid_coop = items_coop ? grid_for(dev, cv, items_coop) : 0;
+    b->grid_field = rebased ? grid_for(dev, cv + 4, rebased) : 0;
     cudaError_t e;
     if ((e = cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice,
                              b->stream)) ||
@@ -822,15 +857,15 @@ cudaError_t batch_enqueue(anacor_batch *b, cudaStream_t st)
 {
     if (b->items <= 0)
         return cudaSuccess;
+    const int cv = b->variant > 4 ? budget_of(b->variant) : b->variant;
     if (b->variant <= 4 || b->n_field == 0)
-        return launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st,
-                                 b->variant > 4 ? b->variant - 4 : b->variant);
+        return launch_absorption(b->d_descs, (int)b->plans.size(), b->items, b->d_counter, b->grid, st, cv);
     cudaError_t e = cudaSuccess;
     if (b->items_coop > 0)
-        e = launch_absorption(b->d_descs, b->n_coop, b->items_coop, b->d_counter, b->grid_coop, st, b->variant - 4);
+        e = launch_absorption(b->d_descs, b->n_coop, b->items_coop, b->d_counter, b->grid_coop, st, cv);
     if (e == cudaSuccess && b->items_field > 0)
         e = launch_absorption(b->d_descs_field, b->n_field, b->items_field, b->d_counter_field, b->grid_field, st,
-                              b->variant);
+                              cv + 4);
     return e;
 }
 
@@ -1079,7 +1114,8 @@ int anacor_plan_count_steps(anacor_plan *p, uint64_t *total)
     return succeed();
 }
 
-int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *out)
+namespace {
+int distance_fields(const int8_t *label, const int64_t *shape, uint8_t *out, bool octants)
 {
     if (!label || !shape || !out)
         return fail(kErrArgs, "null argument");
@@ -1096,11 +1132,13 @@ int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *ou
     int *d_bad = nullptr;
     int bad = 0;
     cudaError_t e;
-    if (!(e = dev_alloc(&d_vol, nvol, st)) && !(e = dev_alloc(&d_out, nvol, st)) && !(e = dev_alloc(&d_tmp, nvol, st)) &&
+    if (!(e = dev_alloc(&d_vol, nvol, st)) && !(e = dev_alloc(&d_out, nvol * (octants ? 8 : 1), st)) &&
+        !(e = dev_alloc(&d_tmp, nvol * (octants ? 6 : 1), st)) &&
         !(e = dev_alloc(&d_bad, 1, st)) &&
         !(e = cudaMemcpyAsync(d_vol, label, nvol, cudaMemcpyHostToDevice, st)) &&
-        !(e = launch_distance_field(d_vol, dims, d_out, d_tmp, d_bad, st)) &&
-        !(e = cudaMemcpyAsync(out, d_out, nvol, cudaMemcpyDeviceToHost, st)) &&
+        !(e = octants ? launch_octant_fields(d_vol, dims, d_out, d_tmp, d_bad, st)
+                   : launch_distance_field(d_vol, dims, d_out, d_tmp, d_bad, st)) &&
+        !(e = cudaMemcpyAsync(out, d_out, nvol * (octants ? 8 : 1), cudaMemcpyDeviceToHost, st)) &&
         !(e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st)))
         e = cudaStreamSynchronize(st);
     dev_free(d_vol, st);
@@ -1112,6 +1150,17 @@ int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *ou
     if (bad)
         return fail(kErrUnsupported, "the distance field needs labels in 0..7");
     return succeed();
+}
+}  // namespace
+
+int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *out)
+{
+    return distance_fields(label, shape, out, false);
+}
+
+int anacor_octant_fields(const int8_t *label, const int64_t *shape, uint8_t *out)
+{
+    return distance_fields(label, shape, out, true);
 }
 
 const double *anacor_plan_device_result(anacor_plan *p) { return p ? p->d_out : nullptr; }
@@ -1165,10 +1214,10 @@ int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream)
     if ((e = cudaMemcpyAsync(d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice, st)))
         return cuda_fail(e, "descriptor upload");
     if (total > 0) {
-        // one launch: the field march only when every sample has its field
-        int variant = p0->variant;
+        // one launch: the field march only when every sample marches on a field
+        int variant = kernel_variant(p0->variant);
         for (int i = 0; i < n_plans && variant > 4; i++)
-            if (plans[i]->field_state != 1)
+            if (!plan_marches_field(plans[i]))
                 variant -= 4;
         const int grid = grid_for(p0->dev, variant, total);
         if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st, variant)))
@@ -1482,7 +1531,7 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
     TuneVal cv{0, 0, 1, 0.0f};
     const bool cached = tune_lookup(p, cv);
     // a cached distance-field choice does not apply to a volume without a field
-    if (cached && (cv.variant <= 4 || plan_ensure_field(p) == kOk)) {
+    if (cached && (cv.variant <= 4 || plan_ensure_field(p, cv.variant > kVariants ? 2 : 1) == kOk)) {
         if (best_ms)
             *best_ms = cv.ms;
         return plan_configure(p, cv.variant, cv.tile, cv.order) ? t_status : succeed();
@@ -1528,8 +1577,10 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
     }
     // the distance-field variants where the labels allow a field
     std::vector<int> variants{2, 3, 4};
-    if (plan_ensure_field(p) == kOk)
+    if (plan_ensure_field(p, 1) == kOk)
         variants.insert(variants.end(), {6, 7, 8});
+    if (plan_ensure_field(p, 2) == kOk)
+        variants.insert(variants.end(), {10, 11, 12});
     for (int tile : {128, 256, 512, 1024, 2048})
         for (int variant : variants) {
             float t = 0.0f;
@@ -1592,7 +1643,7 @@ anacor_batch *anacor_batch_create(anacor_plan *const *plans, int n_plans)
 
 int anacor_batch_configure(anacor_batch *b, int variant)
 {
-    if (!b || variant < 0 || variant > kVariants)
+    if (!b || variant < 0 || variant > kPlanVariants)
         return fail(kErrArgs, "bad arguments");
     b->variant = variant;
     if (int st = batch_upload(b))
@@ -1666,9 +1717,9 @@ int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl)
     float best = 1e30f;
     int best_v = 0;
     std::vector<int> variants{2, 3, 4};
-    bool fields = true;
+    bool fields = false;
     for (anacor_plan *p : b->plans)
-        fields = fields && plan_ensure_field(p) == kOk;
+        fields = fields || plan_marches_field(p);
     if (fields)
         variants.insert(variants.end(), {6, 7, 8});
     cudaEvent_t e0, e1;

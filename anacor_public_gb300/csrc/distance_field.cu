@@ -15,6 +15,13 @@
 //   volume  D(v)     = 1 + max{ r : all |dz| <= r have v's label and d_xy >= r + 1 }
 // Voxels outside the volume do not count (marches never leave it).  The
 // labels must fit 3 bits (0..7); the first pass flags any that do not.
+//
+// Octant fields: the same construction with one-sided scans gives, for each
+// of the 8 sign combinations (sz, sy, sx), 1 + the largest r for which the
+// corner box v + [0..r]^3 * (sz, sy, sx) holds one label.  A ray whose
+// direction has those signs only moves into that box, so behind-the-ray
+// boundaries (the one just crossed) do not shorten its skips.  Layout:
+// [octant][Z][Y][X] with octant = (sx < 0) | (sy < 0) << 1 | (sz < 0) << 2.
 #include "anacor_internal.h"
 #include "trace_launch.h"
 
@@ -24,8 +31,9 @@ namespace {
 constexpr int kFieldCap = 31;
 constexpr int kFieldThreads = 256;
 
-// d_x along each row; one CTA per (z, y) row
-__global__ void __launch_bounds__(kFieldThreads) field_rows(const int8_t *__restrict__ vol, int dx,
+// d_x along each row (dir 0: both sides, +1 / -1: ahead / behind only); one
+// CTA per (z, y) row
+__global__ void __launch_bounds__(kFieldThreads) field_rows(const int8_t *__restrict__ vol, int dx, int dir,
                                                             uint8_t *__restrict__ out, int *__restrict__ bad)
 {
     const long long row = (long long)blockIdx.x * dx;
@@ -41,7 +49,7 @@ __global__ void __launch_bounds__(kFieldThreads) field_rows(const int8_t *__rest
             } else if (lab != 0) {
                 int d = kFieldCap;
                 for (int k = 1; k < kFieldCap; k++) {
-                    if ((x + k < dx && r[x + k] != lab) || (x - k >= 0 && r[x - k] != lab)) {
+                    if ((dir >= 0 && x + k < dx && r[x + k] != lab) || (dir <= 0 && x - k >= 0 && r[x - k] != lab)) {
                         d = k;
                         break;
                     }
@@ -59,7 +67,7 @@ __global__ void __launch_bounds__(kFieldThreads) field_rows(const int8_t *__rest
 // (coordinate `c` of the row's voxels on that axis): in holds label | d << 3
 // of the previous pass, out receives label | d' << 3.
 __global__ void __launch_bounds__(kFieldThreads) field_grow(const uint8_t *__restrict__ in, int dy, int dx,
-                                                            int axis, int n, long long stride,
+                                                            int axis, int n, long long stride, int dir,
                                                             uint8_t *__restrict__ out)
 {
     const long long row = (long long)blockIdx.x * dx;
@@ -78,11 +86,11 @@ __global__ void __launch_bounds__(kFieldThreads) field_grow(const uint8_t *__res
         uint32_t m = b >> 3;
         int d = 1;
         for (int r = 1; r < kFieldCap; r++) {
-            if (c + r < n) {
+            if (dir >= 0 && c + r < n) {
                 const uint32_t u = in[v + r * stride];
                 m = min(m, (u & 7u) == lab ? (u >> 3) : 0u);
             }
-            if (c - r >= 0) {
+            if (dir <= 0 && c - r >= 0) {
                 const uint32_t u = in[v - r * stride];
                 m = min(m, (u & 7u) == lab ? (u >> 3) : 0u);
             }
@@ -106,9 +114,36 @@ cudaError_t launch_distance_field(const int8_t *d_vol, const int *dims, uint8_t 
     if (e != cudaSuccess)
         return e;
     const long long plane = (long long)dims[1] * dims[2];
-    field_rows<<<rows, kFieldThreads, 0, st>>>(d_vol, dims[2], d_out, d_bad);
-    field_grow<<<rows, kFieldThreads, 0, st>>>(d_out, dims[1], dims[2], 1, dims[1], dims[2], d_tmp);
-    field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp, dims[1], dims[2], 0, dims[0], plane, d_out);
+    field_rows<<<rows, kFieldThreads, 0, st>>>(d_vol, dims[2], 0, d_out, d_bad);
+    field_grow<<<rows, kFieldThreads, 0, st>>>(d_out, dims[1], dims[2], 1, dims[1], dims[2], 0, d_tmp);
+    field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp, dims[1], dims[2], 0, dims[0], plane, 0, d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_octant_fields(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
+                                 cudaStream_t st)
+{
+    const unsigned rows = (unsigned)dims[0] * (unsigned)dims[1];
+    if (rows == 0 || dims[2] == 0)
+        return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+    if (e != cudaSuccess)
+        return e;
+    const long long plane = (long long)dims[1] * dims[2];
+    const long long nvol = plane * dims[0];
+    // tmp[0..1]: rows ahead (+x) / behind (-x); tmp[2 + 2*by + bx]: planes
+    for (int bx = 0; bx < 2; bx++)
+        field_rows<<<rows, kFieldThreads, 0, st>>>(d_vol, dims[2], bx ? -1 : 1, d_tmp + bx * nvol, d_bad);
+    for (int by = 0; by < 2; by++)
+        for (int bx = 0; bx < 2; bx++)
+            field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp + bx * nvol, dims[1], dims[2], 1, dims[1], dims[2],
+                                                       by ? -1 : 1, d_tmp + (2 + 2 * by + bx) * nvol);
+    for (int bz = 0; bz < 2; bz++)
+        for (int by = 0; by < 2; by++)
+            for (int bx = 0; bx < 2; bx++)
+                field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp + (2 + 2 * by + bx) * nvol, dims[1], dims[2], 0,
+                                                           dims[0], plane, bz ? -1 : 1,
+                                                           d_out + (bx | by << 1 | bz << 2) * nvol);
     return cudaGetLastError();
 }
 

@@ -177,6 +177,9 @@ void face_rule(int face, double th, double ph, FaceRule &r)
             r.exact_mask |= uint8_t(1u << a);
     }
     r.fast = fast;
+    // signs of the march direction: the count axis steps by q = +-1, the
+    // others by their ratios (a zero ratio counts as positive)
+    r.octant = uint8_t((r.q[2] < 0) | (r.q[1] < 0) << 1 | (r.q[0] < 0) << 2);
     // never above 2^16 / qmax: the device's skip (D - 2) * skip_rq >> 16 stays
     // within floor((D - 2) / qmax)
     const double qmax = std::max(std::fabs(r.q[r.count_axis == 0 ? 1 : 0]), std::fabs(r.q[r.count_axis == 2 ? 1 : 2]));

@@ -63,6 +63,7 @@ struct Vol {
     const int8_t *p;
     int dz, dy, dx;
     const uint8_t *field = nullptr;   // label | distance << 3, for the distance-field march
+    long long field_stride = 0;       // 0: one centred field; else 8 octant fields this far apart
 };
 
 __device__ __forceinline__ int pick3(int k, int z, int y, int x)
@@ -366,7 +367,8 @@ __device__ __forceinline__ int wall_increments(double q, int c, int h)
 // One lane's field march over one leg, as a chain of dependent loads.
 struct FieldChain {
     const FaceRule *R;
-    const uint8_t *pk;        // field + the leg's start voxel
+    const uint8_t *fld;       // the field this leg marches on (its octant's)
+    const uint8_t *pk;        // fld + the leg's start voxel
     long long off, Qa, Qb;
     uint32_t Ma, Mb, rq;
     int dS, Sa, Sb;           // strides of the step axis (signed) and the two others
@@ -379,11 +381,12 @@ __device__ __forceinline__ int field_nmax(uint32_t d, uint32_t rq)
     return d < 2u ? 0 : min((int)d - 1, (int)(((d - 2u) * rq) >> 16));
 }
 
-__device__ __forceinline__ void chain_init(FieldChain &c, const FaceRule &R, const LegGeom &g, const Vol &v, int base,
-                                           int lim, uint32_t b0, const March &m)
+__device__ __forceinline__ void chain_init(FieldChain &c, const FaceRule &R, const LegGeom &g, const uint8_t *fld,
+                                           int base, int lim, uint32_t b0, const March &m)
 {
     c.R = &R;
-    c.pk = v.field + base;
+    c.fld = fld;
+    c.pk = fld + base;
     c.off = g.off;
     c.Qa = g.Qa;
     c.Qb = g.Qb;
@@ -406,7 +409,7 @@ __device__ __forceinline__ uint32_t chain_load(const FieldChain &c, int cz, int 
 {
     const long long ea = c.off + (long long)c.i * c.Qa, eb = c.off + (long long)c.i * c.Qb;
     if (((uint32_t)ea + c.Ma < 2u * c.Ma) | ((uint32_t)eb + c.Mb < 2u * c.Mb))
-        return exact_byte(*c.R, cz, cy, cx, c.i, v, v.field);
+        return exact_byte(*c.R, cz, cy, cx, c.i, v, c.fld);
     return __ldg(c.pk + (c.i * c.dS + (int)(ea >> 32) * c.Sa + (int)(eb >> 32) * c.Sb));
 }
 
@@ -442,11 +445,11 @@ __device__ __forceinline__ void chain_done(const FieldChain &c, March &m)
 }
 
 __device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx,
-                                            const Vol &v, int base, int lim, uint32_t b0, March &m, bool &stopped,
-                                            uint16_t *seg)
+                                            const Vol &v, const uint8_t *fld, int base, int lim, uint32_t b0,
+                                            March &m, bool &stopped, uint16_t *seg)
 {
     FieldChain c;
-    chain_init(c, R, g, v, base, lim, b0, m);
+    chain_init(c, R, g, fld, base, lim, b0, m);
     while (c.on)
         chain_step(c, chain_load(c, cz, cy, cx, v), seg, stopped);
     chain_done(c, m);
@@ -581,14 +584,15 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
             if (kField) {
                 // per lane, no warp synchronisation: the field march (now, or
                 // by the caller together with the other leg)
-                b0 = __ldg(v.field + base);
+                const uint8_t *fld = v.field + R.octant * v.field_stride;
+                b0 = __ldg(fld + base);
                 if ((b0 & 7u) == 0) {
                     stopped = true;
                 } else {
                     m.prev = (int)(b0 & 7u);
                     live = lim > 1;
                     if (kMarchNow && live)
-                        field_march(R, g, cz, cy, cx, v, base, lim, b0, m, stopped, seg);
+                        field_march(R, g, cz, cy, cx, v, fld, base, lim, b0, m, stopped, seg);
                 }
             } else {
                 const int lab0 = __ldg(v.p + base);
@@ -991,7 +995,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         }
         __syncwarp();
 
-        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field};
+        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field, D.field_stride};
         float s = 0.0f, c = 0.0f;
         int bad = kOk;
         unsigned nsteps = 0;

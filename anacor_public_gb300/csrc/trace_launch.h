@@ -45,6 +45,7 @@ struct SampleDesc {
     const double *qtab;     // optional quotient table covering den <= max(dim)
     long long work_begin;   // first global work item of this sample
     const uint8_t *field;   // label | distance << 3 (launch_distance_field); required by variants 5..8
+    long long field_stride; // 0: one centred field; volume size: 8 octant fields (launch_octant_fields)
 };
 
 // Absorption map of one sample (gridding mode): for every grid direction d and
@@ -128,6 +129,10 @@ cudaError_t launch_order_permutation(const long long *d_c, int n, const int *dim
 // *d_bad becomes nonzero when a label lies outside 0..7 (no field then).
 cudaError_t launch_distance_field(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
                                   cudaStream_t st);
+// The 8 octant fields ([octant][Z][Y][X], octant = (sx<0) | (sy<0)<<1 | (sz<0)<<2):
+// d_out holds 8 volumes, d_tmp 6.
+cudaError_t launch_octant_fields(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
+                                 cudaStream_t st);
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs
 // take items from `d_counter` (reset inside the launch sequence).
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,

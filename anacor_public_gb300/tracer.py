@@ -280,3 +280,14 @@ def distance_field(label) -> np.ndarray:
     out = np.zeros(label.shape, np.uint8)
     _lib.check(L.anacor_distance_field(label, np.array(label.shape, dtype=np.int64), out), L)
     return out
+
+
+def octant_fields(label) -> np.ndarray:
+    """The 8 octant fields of kernel variants 9..12, [octant][Z][Y][X] uint8:
+    (label & 7) | (min(r + 1, 31) << 3), r the largest corner box toward the
+    octant's signs (octant = (sx<0) | (sy<0)<<1 | (sz<0)<<2) holding one label."""
+    L = _lib.load()
+    label = _c(label, np.int8)
+    out = np.zeros((8,) + label.shape, np.uint8)
+    _lib.check(L.anacor_octant_fields(label, np.array(label.shape, dtype=np.int64), out), L)
+    return out

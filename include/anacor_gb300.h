@@ -144,8 +144,9 @@ int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *c
  * variant = kernel variant: 1..4 the warp-cooperative march compiled for
  * 1..4 CTAs per SM, 5..8 the same register budgets with the distance-field
  * march (steps over increments that a chessboard distance field proves to
- * keep the label; needs labels in 0..7, else kErrUnsupported), 0 = process
- * default; tile = voxels per work item
+ * keep the label; needs labels in 0..7, else kErrUnsupported), 9..12 the
+ * same on the 8 octant fields (each leg reads the field of its direction's
+ * octant), 0 = process default; tile = voxels per work item
  * (>= 128, 0 = unchanged); order = voxel order of the packed list: 0 the
  * caller's, 1 Morton (Z-order) of (z, y, x), 2..7 blocked (Morton order of
  * blocks of 1x2x16, 1x4x8, 2x4x32, 4x8x64, 4x16x32 or 8x16x128 voxels, row
@@ -157,6 +158,11 @@ int anacor_plan_configure(anacor_plan *p, int variant, int tile, int order);
  * voxels).  kErrUnsupported when a label lies outside 0..7.  No counterpart
  * in the reference. */
 int anacor_distance_field(const int8_t *label, const int64_t *shape, uint8_t *out);
+/* The 8 octant fields variants 9..12 march on: out[o][v] (8 volumes,
+ * o = (sx < 0) | (sy < 0) << 1 | (sz < 0) << 2) = (label & 7) | (min(r + 1, 31) << 3),
+ * r the largest box v + [0..r]^3 * (sz, sy, sx) (clipped to the volume) that
+ * holds one label; 0 for label-0 voxels.  No counterpart in the reference. */
+int anacor_octant_fields(const int8_t *label, const int64_t *shape, uint8_t *out);
 int anacor_plan_config(const anacor_plan *p, int *variant, int *tile, int *order);
 /* Autotuner: times every (variant, tile, order) candidate on the first
  * reflections of the plan (at least sample_refl of them) and keeps the

@@ -49,6 +49,31 @@ def field_cpu(label):
     return out.astype(np.uint8)
 
 
+def octant_fields_cpu(label):
+    """[octant][Z][Y][X]: (label & 7) | (min(r + 1, 31) << 3), r the largest
+    corner box toward the octant's signs holding one label; 0 for label 0."""
+    lab = label.astype(np.int16)
+    out = np.zeros((8,) + lab.shape, np.uint8)
+    for o in range(8):
+        signs = (-1 if o & 4 else 1, -1 if o & 2 else 1, -1 if o & 1 else 1)   # z, y, x
+        D = np.ones(lab.shape, np.int32)
+        alive = np.ones(lab.shape, bool)
+        for r in range(1, 31):
+            size = r + 1
+            # window over offsets 0..r toward each sign
+            origin = [-(size // 2) if sg > 0 else (size - 1) - size // 2 for sg in signs]
+            mx = nd.maximum_filter(lab, size=size, origin=origin, mode="nearest")
+            mn = nd.minimum_filter(lab, size=size, origin=origin, mode="nearest")
+            alive &= (mx == lab) & (mn == lab)
+            if not alive.any():
+                break
+            D[alive] = r + 1
+        f = (lab & 7) | (D << 3)
+        f[lab == 0] = 0
+        out[o] = f.astype(np.uint8)
+    return out
+
+
 def blocky_volume(shape, seed, n_boxes=40, labels=(1, 2, 3, 4, 5, 6, 7)):
     rng = np.random.default_rng(seed)
     vol = np.zeros(shape, np.int8)
@@ -63,6 +88,16 @@ def blocky_volume(shape, seed, n_boxes=40, labels=(1, 2, 3, 4, 5, 6, 7)):
 def test_field_matches_cpu(shape, seed):
     vol = blocky_volume(shape, seed)
     assert np.array_equal(tracer.distance_field(vol), field_cpu(vol))
+
+
+@pytest.mark.parametrize("shape,seed", [((20, 33, 47), 5), ((9, 70, 5), 6), ((1, 1, 90), 7)])
+def test_octant_fields_match_cpu(shape, seed):
+    vol = blocky_volume(shape, seed)
+    assert np.array_equal(tracer.octant_fields(vol), octant_fields_cpu(vol))
+
+
+def test_octant_fields_of_a_sample_volume(small):
+    assert np.array_equal(tracer.octant_fields(small.label), octant_fields_cpu(small.label))
 
 
 def test_field_of_a_sample_volume(small):
@@ -98,7 +133,7 @@ def want(sample, oracle):
     return oracle.overall(sample, threads=os.cpu_count() or 1)
 
 
-@pytest.mark.parametrize("variant", [5, 6, 7, 8])
+@pytest.mark.parametrize("variant", [5, 6, 7, 8, 9, 10, 11, 12])
 @pytest.mark.parametrize("tile,order", [(512, 1), (2048, 0), (128, 3)])
 def test_field_variants_match_the_oracle_and_the_cooperative_march(sample, want, variant, tile, order):
     p = tracer.Plan.from_sample(sample)
@@ -108,18 +143,19 @@ def test_field_variants_match_the_oracle_and_the_cooperative_march(sample, want,
     a = p.result()
     assert max_rel(a, want) <= RTOL
     steps = p.count_steps()
-    p.configure(variant - 4, tile, order)
+    p.configure((variant - 1) % 4 + 1, tile, order)
     p.run()
     assert np.array_equal(p.result(), a)
     assert p.count_steps() == steps
     p.close()
 
 
-def test_field_march_beamline_vs_golden(golden_dir):
+@pytest.mark.parametrize("variant", [8, 12])
+def test_field_march_beamline_vs_golden(golden_dir, variant):
     gold = np.load(os.path.join(golden_dir, "beamline_ah.npz"))["ah"]
     b = synth.beamline_sample(n_refl=12)
     p = tracer.Plan.from_sample(b)
-    p.configure(8, 1024, 1)
+    p.configure(variant, 1024, 1)
     p.run()
     a = p.result()
     assert max_rel(a, gold) <= RTOL
@@ -160,10 +196,11 @@ def test_field_march_on_wall_and_slab_volumes(oracle):
         t = synth.Sample(label=vol, coords=coords, s1=s.s1, omega=s.omega, xray=s.xray, omega_axis=s.omega_axis,
                          F=s.F, voxel=s.voxel, mu=s.mu)
         ref = oracle.overall(t, threads=4)
-        a8, n8 = _run(t, 8)
         a4, n4 = _run(t, 4)
-        assert max_rel(a8, ref) <= RTOL
-        assert np.array_equal(a8, a4) and n8 == n4
+        for v in (8, 12):
+            a8, n8 = _run(t, v)
+            assert max_rel(a8, ref) <= RTOL
+            assert np.array_equal(a8, a4) and n8 == n4
 
 
 def test_field_variant_refused_for_wide_labels(sample):
@@ -171,9 +208,10 @@ def test_field_variant_refused_for_wide_labels(sample):
     vol[0, 0, 0] = 12
     p = tracer.Plan(vol, sample.coords, sample.voxel, sample.mu)
     p.set_reflections(sample.s1[:8], sample.omega[:8], sample.xray, sample.omega_axis, sample.F)
-    with pytest.raises(_lib.AnacorError) as e:
-        p.configure(8, 512, 1)
-    assert e.value.status == K_UNSUPPORTED
+    for v in (8, 12):
+        with pytest.raises(_lib.AnacorError) as e:
+            p.configure(v, 512, 1)
+        assert e.value.status == K_UNSUPPORTED
     p.autotune()
     assert p.config()["variant"] in (2, 3, 4)
     p.close()
@@ -190,7 +228,7 @@ def test_batch_splits_field_and_cooperative_samples(oracle):
     wants = [oracle.overall(s, threads=os.cpu_count() or 1) for s in samples]
     plans = [tracer.Plan.from_sample(s) for s in samples]
     plans[0].configure(8, 512, 1)
-    plans[1].configure(4, 512, 1)
+    plans[1].configure(12, 512, 1)   # octant fields, in the same field launch
     plans[2].configure(4, 512, 1)
     b = tracer.Batch(plans)
     st = torch.cuda.Stream()

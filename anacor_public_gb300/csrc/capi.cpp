@@ -223,6 +223,8 @@ struct anacor_plan {
     int sq_stride = 0;
     const double *d_qtab = nullptr;  // device quotient table (owned by the device state)
     ReflTable *h_refl = nullptr;   // pinned staging
+    int *d_order = nullptr;        // processing order of the reflections (grouped by direction octants)
+    std::vector<int> h_order;
     int64_t n_refl = 0, refl_cap = 0;
     size_t partial_cap = 0;        // entries of d_partial (refl_cap * tiles)
     int tiles = 0;
@@ -255,6 +257,7 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_c64, st);
     dev_free(p->d_field, st);
     dev_free(p->d_field8, st);
+    dev_free(p->d_order, st);
     if (p->h_refl)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
@@ -431,6 +434,7 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
         dev_free(p->d_out, st);
         dev_free(p->d_partial, st);
         dev_free(p->d_arrive, st);
+        dev_free(p->d_order, st);
         if (p->h_refl) {
             cudaStreamSynchronize(st);
             cudaFreeHost(p->h_refl);
@@ -438,7 +442,7 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
         }
         p->partial_cap = 0;
         if ((e = dev_alloc(&p->d_refl, (size_t)n_refl, st)) || (e = dev_alloc(&p->d_out, (size_t)n_refl, st)) ||
-            (e = dev_alloc(&p->d_arrive, (size_t)n_refl, st)))
+            (e = dev_alloc(&p->d_arrive, (size_t)n_refl, st)) || (e = dev_alloc(&p->d_order, (size_t)n_refl, st)))
             return cuda_fail(e, "device allocation");
         if ((e = cudaMemsetAsync(p->d_arrive, 0, (size_t)n_refl * sizeof(unsigned), st)))
             return cuda_fail(e, "cudaMemset");
@@ -526,6 +530,7 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     d.sq_stride = p->sq_stride;
     d.qtab = p->d_qtab;
     d.work_begin = work_begin;
+    d.order = p->n_refl > 0 ? p->d_order : nullptr;
     if (p->variant > kVariants) {
         d.field = p->field8_state == 1 ? p->d_field8 : nullptr;
         d.field_stride = (long long)p->dims[0] * p->dims[1] * p->dims[2];
@@ -549,14 +554,31 @@ int plan_upload_desc(anacor_plan *p, unsigned long long *steps)
     return kOk;
 }
 
-// upload the staged tables and the plan's own one-sample descriptor
+// Upload the staged tables, the processing order and the plan's own
+// one-sample descriptor.  Reflections are processed grouped by the direction
+// octants of their two legs (a stable counting sort on 6 bits), so that the
+// work items in flight at one time read the same two of the 8 octant fields
+// (and nearby parts of the volume); results stay in the caller's order.
 int plan_upload_tables(anacor_plan *p)
 {
     cudaError_t e;
-    if (p->n_refl > 0 &&
-        (e = cudaMemcpyAsync(p->d_refl, p->h_refl, (size_t)p->n_refl * sizeof(ReflTable), cudaMemcpyHostToDevice,
-                             p->stream)))
-        return cuda_fail(e, "table upload");
+    const int64_t n = p->n_refl;
+    if (n > 0) {
+        int count[65] = {0};
+        auto key = [&](int64_t r) { return p->h_refl[r].rule[0][0].octant | p->h_refl[r].rule[1][0].octant << 3; };
+        for (int64_t r = 0; r < n; r++)
+            count[key(r) + 1]++;
+        for (int k = 0; k < 64; k++)
+            count[k + 1] += count[k];
+        p->h_order.resize((size_t)n);
+        for (int64_t r = 0; r < n; r++)
+            p->h_order[(size_t)count[key(r)]++] = (int)r;
+        if ((e = cudaMemcpyAsync(p->d_refl, p->h_refl, (size_t)n * sizeof(ReflTable), cudaMemcpyHostToDevice,
+                                 p->stream)) ||
+            (e = cudaMemcpyAsync(p->d_order, p->h_order.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice,
+                                 p->stream)))
+            return cuda_fail(e, "table upload");
+    }
     return plan_upload_desc(p, nullptr);
 }
 

@@ -984,8 +984,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             continue;
         }
         const long long local = item - D.work_begin;
-        const long long r = local / D.tiles;
-        const int t = (int)(local - r * D.tiles);
+        const long long k = local / D.tiles;
+        const long long r = D.order ? (long long)__ldg(D.order + k) : k;
+        const int t = (int)(local - k * D.tiles);
         __syncwarp();   // the previous item's reads of the table are done
         {
             const int4 *src = reinterpret_cast<const int4 *>(D.refl + r);
@@ -1227,8 +1228,9 @@ __global__ void __launch_bounds__(kBlock, 2) bisection_kernel(const SampleDesc *
         const int si = find_sample(descs, n_desc, item);
         const SampleDesc &D = descs[si];
         const long long local = item - D.work_begin;
-        const long long r = local / D.tiles;
-        const int t = (int)(local - r * D.tiles);
+        const long long k = local / D.tiles;
+        const long long r = D.order ? (long long)__ldg(D.order + k) : k;
+        const int t = (int)(local - k * D.tiles);
         {
             const int4 *src = reinterpret_cast<const int4 *>(D.refl + r);
             int4 *dst = reinterpret_cast<int4 *>(&tab);

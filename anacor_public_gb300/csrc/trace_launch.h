@@ -46,6 +46,7 @@ struct SampleDesc {
     long long work_begin;   // first global work item of this sample
     const uint8_t *field;   // label | distance << 3 (launch_distance_field); required by variants 5..8
     long long field_stride; // 0: one centred field; volume size: 8 octant fields (launch_octant_fields)
+    const int *order;       // optional [n_refl]: the k-th reflection processed (octant-sorted), else k
 };
 
 // Absorption map of one sample (gridding mode): for every grid direction d and

@@ -102,6 +102,95 @@ __global__ void __launch_bounds__(kFieldThreads) field_grow(const uint8_t *__res
     }
 }
 
+// Octant passes, every sign at once (independent scans interleaved per thread).
+// Rows: out[0] looks ahead (+x), out[1] behind (-x).
+__global__ void __launch_bounds__(kFieldThreads) octant_rows(const int8_t *__restrict__ vol, int dx, long long nvol,
+                                                             uint8_t *__restrict__ out, int *__restrict__ bad)
+{
+    const long long row = (long long)blockIdx.x * dx;
+    const int8_t *r = vol + row;
+    bool any_bad = false;
+    for (int x0 = 0; x0 < dx; x0 += kFieldThreads) {
+        const int x = x0 + (int)threadIdx.x;
+        if (x < dx) {
+            const int lab = r[x];
+            uint8_t o0 = 0, o1 = 0;
+            if ((unsigned)lab > 7u) {
+                any_bad = true;
+            } else if (lab != 0) {
+                int d0 = kFieldCap, d1 = kFieldCap;
+                for (int k = 1; k < kFieldCap && (d0 == kFieldCap || d1 == kFieldCap); k++) {
+                    if (d0 == kFieldCap && x + k < dx && r[x + k] != lab)
+                        d0 = k;
+                    if (d1 == kFieldCap && x - k >= 0 && r[x - k] != lab)
+                        d1 = k;
+                }
+                o0 = (uint8_t)(lab | (d0 << 3));
+                o1 = (uint8_t)(lab | (d1 << 3));
+            }
+            out[row + x] = o0;
+            out[nvol + row + x] = o1;
+        }
+    }
+    if (__syncthreads_or(any_bad) && threadIdx.x == 0)
+        atomicOr(bad, 1);
+}
+
+// Growth along one axis (stride, extent n) of kIn one-sided inputs at once,
+// each toward both signs: result j = 2 * i + s (s = 0 toward +, 1 toward -)
+// from in[i], stored as out[j], or (kOctants, i = 2 * bx + by, s = bz) as
+// out[bx | by << 1 | bz << 2]; inputs and outputs are volumes nvol apart.
+template <int kIn, bool kOctants>
+__global__ void __launch_bounds__(kFieldThreads) octant_grow(const uint8_t *__restrict__ in, int dy, int dx,
+                                                             int axis, int n, long long stride, long long nvol,
+                                                             uint8_t *__restrict__ out)
+{
+    const long long row = (long long)blockIdx.x * dx;
+    const int c = axis == 1 ? (int)(blockIdx.x % (unsigned)dy) : (int)(blockIdx.x / (unsigned)dy);
+    for (int x0 = 0; x0 < dx; x0 += kFieldThreads) {
+        const int x = x0 + (int)threadIdx.x;
+        if (x >= dx)
+            continue;
+        const long long v = row + x;
+        const uint32_t lab = in[v] & 7u;
+        if (lab == 0) {
+#pragma unroll
+            for (int j = 0; j < 2 * kIn; j++)
+                out[(kOctants ? ((j >> 2) | (((j >> 1) & 1) << 1) | ((j & 1) << 2)) : j) * nvol + v] = 0;
+            continue;
+        }
+        uint32_t m[2 * kIn];
+        int d[2 * kIn];
+#pragma unroll
+        for (int i = 0; i < kIn; i++) {
+            m[2 * i] = m[2 * i + 1] = in[i * nvol + v] >> 3;
+            d[2 * i] = d[2 * i + 1] = 1;
+        }
+        unsigned live = (1u << (2 * kIn)) - 1u;
+        for (int r = 1; r < kFieldCap && live; r++) {
+            const bool up = c + r < n, down = c - r >= 0;
+#pragma unroll
+            for (int j = 0; j < 2 * kIn; j++) {
+                if (!((live >> j) & 1u))
+                    continue;
+                const bool plus = (j & 1) == 0;
+                if (plus ? up : down) {
+                    const uint32_t u = in[(j >> 1) * nvol + v + (plus ? r : -r) * stride];
+                    m[j] = min(m[j], (u & 7u) == lab ? (u >> 3) : 0u);
+                }
+                if (m[j] < (uint32_t)(r + 1))
+                    live &= ~(1u << j);
+                else
+                    d[j] = r + 1;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 2 * kIn; j++)
+            out[(kOctants ? ((j >> 2) | (((j >> 1) & 1) << 1) | ((j & 1) << 2)) : j) * nvol + v] =
+                (uint8_t)(lab | (uint32_t)d[j] << 3);
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_distance_field(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
@@ -131,19 +220,12 @@ cudaError_t launch_octant_fields(const int8_t *d_vol, const int *dims, uint8_t *
         return e;
     const long long plane = (long long)dims[1] * dims[2];
     const long long nvol = plane * dims[0];
-    // tmp[0..1]: rows ahead (+x) / behind (-x); tmp[2 + 2*by + bx]: planes
-    for (int bx = 0; bx < 2; bx++)
-        field_rows<<<rows, kFieldThreads, 0, st>>>(d_vol, dims[2], bx ? -1 : 1, d_tmp + bx * nvol, d_bad);
-    for (int by = 0; by < 2; by++)
-        for (int bx = 0; bx < 2; bx++)
-            field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp + bx * nvol, dims[1], dims[2], 1, dims[1], dims[2],
-                                                       by ? -1 : 1, d_tmp + (2 + 2 * by + bx) * nvol);
-    for (int bz = 0; bz < 2; bz++)
-        for (int by = 0; by < 2; by++)
-            for (int bx = 0; bx < 2; bx++)
-                field_grow<<<rows, kFieldThreads, 0, st>>>(d_tmp + (2 + 2 * by + bx) * nvol, dims[1], dims[2], 0,
-                                                           dims[0], plane, bz ? -1 : 1,
-                                                           d_out + (bx | by << 1 | bz << 2) * nvol);
+    // tmp[bx]: rows (bx = 1: -x); tmp[2 + 2*bx + by]: squares; out[bx | by << 1 | bz << 2]
+    octant_rows<<<rows, kFieldThreads, 0, st>>>(d_vol, dims[2], nvol, d_tmp, d_bad);
+    octant_grow<2, false><<<rows, kFieldThreads, 0, st>>>(d_tmp, dims[1], dims[2], 1, dims[1], dims[2], nvol,
+                                                          d_tmp + 2 * nvol);
+    octant_grow<4, true><<<rows, kFieldThreads, 0, st>>>(d_tmp + 2 * nvol, dims[1], dims[2], 0, dims[0], plane, nvol,
+                                                         d_out);
     return cudaGetLastError();
 }
 

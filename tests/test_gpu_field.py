@@ -252,3 +252,19 @@ def test_batch_splits_field_and_cooperative_samples(oracle):
     b.close()
     for p in plans:
         p.close()
+
+
+def test_field_variants_with_full_iteration_and_no_exp(small, oracle):
+    s = small.subset(refl=slice(0, 24))
+    for full, ie in ((1, 1), (0, 0), (1, 0)):
+        ref = oracle.overall(s, threads=os.cpu_count() or 1, full_iteration=full, is_exp=ie)
+        got = {}
+        for v in (4, 8, 12):
+            p = tracer.Plan(s.label, s.coords, s.voxel, s.mu, full_iteration=full, is_exp=ie)
+            p.set_reflections(s.s1, s.omega, s.xray, s.omega_axis, s.F)
+            p.configure(v, 512, 1)
+            p.run()
+            got[v] = p.result()
+            p.close()
+            assert max_rel(got[v], ref) <= RTOL, (full, ie, v)
+        assert np.array_equal(got[8], got[4]) and np.array_equal(got[12], got[4])

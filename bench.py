@@ -191,13 +191,14 @@ def measured_peak_gbs():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
-    """DRAM bytes per absorption launch from the committed ncu summary, if any."""
+def profiled_traffic(workload: str, key: str = "traffic_bytes_per_launch"):
+    """A figure of the committed ncu summary of the absorption kernel (`key: value`
+    line; DRAM bytes per launch by default), if any."""
     p = os.path.join(ROOT, "profiles", f"absorption_kernel_{workload}.md")
     if not os.path.exists(p):
         return None
     for ln in open(p):
-        if ln.strip().startswith("traffic_bytes_per_launch:"):
+        if ln.strip().startswith(key + ":"):
             try:
                 return float(ln.split(":", 1)[1])
             except ValueError:
@@ -388,11 +389,15 @@ def run_ours(args):
         alg_bytes = total_steps * 1 + sum(s.n_refl * len(s.coords) for s in samples) * 12
         achieved = alg_bytes / (ms_step / 1e3) / 1e9
         traffic = profiled_traffic(args.workload)
+        lts = profiled_traffic(args.workload, "lts_bytes_per_launch")
+        lts_pct = profiled_traffic(args.workload, "lts_throughput_pct")
         cpu = None if args.no_cpu_baseline else cpu_baseline(samples, args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": "reflections/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "arith": "u8 labels, int32/32.32 fixed-point march (FP64 where a step is near a rounding boundary), "
+                     "FP32 lengths and exp, FP64 reflection set-up and partial sums",
             "config": {"workload": WORKLOADS[args.workload], "n_samples": len(samples), "n_voxels": n_vox,
                        "n_reflections": n_refl, "volume": [list(s.label.shape) for s in samples][:3],
                        "l2": "flushed between steps (256 MiB write)", "grid": grid, "block": 256,
@@ -400,7 +405,10 @@ def run_ours(args):
             "voxel_rays_per_s": 2.0 * sum(s.n_refl * len(s.coords) for s in samples) * world / (ms_step / 1e3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": src, "traffic": traffic,
-                         "alg_bytes_per_launch": alg_bytes, "label_steps_per_launch": total_steps},
+                         "alg_bytes_per_launch": alg_bytes, "label_steps_per_launch": total_steps,
+                         # the level the label gathers are served from (ncu summary in profiles/)
+                         "l2": {"traffic": lts, "achieved_gbs": (lts / (ms_step / 1e3) / 1e9) if lts else None,
+                                "lts_throughput_pct": lts_pct}},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,

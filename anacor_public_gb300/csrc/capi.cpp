@@ -223,6 +223,7 @@ struct anacor_plan {
     int sq_stride = 0;
     const double *d_qtab = nullptr;  // device quotient table (owned by the device state)
     ReflTable *h_refl = nullptr;   // pinned staging
+    bool h_refl_borrowed = false;  // h_refl is the calling thread's staging buffer (one-call plans)
     int *d_order = nullptr;        // processing order of the reflections (grouped by direction octants)
     std::vector<int> h_order;
     int64_t n_refl = 0, refl_cap = 0;
@@ -258,10 +259,40 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_field, st);
     dev_free(p->d_field8, st);
     dev_free(p->d_order, st);
-    if (p->h_refl)
+    if (p->h_refl && !p->h_refl_borrowed)
         cudaFreeHost(p->h_refl);
     p->h_refl = nullptr;
     cudaStreamSynchronize(st);
+}
+
+// Pinned staging for the reflection tables of one-call plans (the drop-in
+// entry points), kept per thread and grown on demand: a pinned allocation and
+// release per call cost more than the set-up of a few hundred reflections.
+ReflTable *thread_staging(int64_t n_refl)
+{
+    struct Staging {
+        ReflTable *p = nullptr;
+        int64_t cap = 0;
+        ~Staging()
+        {
+            if (p)
+                cudaFreeHost(p);
+        }
+    };
+    static thread_local Staging s;
+    if (n_refl > s.cap) {
+        if (s.p)
+            cudaFreeHost(s.p);
+        s.p = nullptr;
+        s.cap = 0;
+        const int64_t cap = std::max<int64_t>(n_refl, 1024);
+        if (cudaMallocHost(reinterpret_cast<void **>(&s.p), (size_t)cap * sizeof(ReflTable)) != cudaSuccess) {
+            s.p = nullptr;
+            return nullptr;
+        }
+        s.cap = cap;
+    }
+    return s.p;
 }
 
 // the tile actually used: at least `tile`, and large enough that a reflection
@@ -435,7 +466,7 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
         dev_free(p->d_partial, st);
         dev_free(p->d_arrive, st);
         dev_free(p->d_order, st);
-        if (p->h_refl) {
+        if (p->h_refl && !p->h_refl_borrowed) {
             cudaStreamSynchronize(st);
             cudaFreeHost(p->h_refl);
             p->h_refl = nullptr;
@@ -446,7 +477,8 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
             return cuda_fail(e, "device allocation");
         if ((e = cudaMemsetAsync(p->d_arrive, 0, (size_t)n_refl * sizeof(unsigned), st)))
             return cuda_fail(e, "cudaMemset");
-        if ((e = cudaMallocHost(reinterpret_cast<void **>(&p->h_refl), (size_t)n_refl * sizeof(ReflTable))))
+        if (!p->h_refl_borrowed &&
+            (e = cudaMallocHost(reinterpret_cast<void **>(&p->h_refl), (size_t)n_refl * sizeof(ReflTable))))
             return cuda_fail(e, "pinned allocation");
         p->refl_cap = n_refl;
     }
@@ -652,8 +684,15 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
 {
     anacor_plan p;
     int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
-    if (!st)
+    if (!st) {
+        // the tables go through this thread's pinned staging (no pinned
+        // allocation per call); the plan lives for this call only
+        p.h_refl = thread_staging(n_refl);
+        p.h_refl_borrowed = p.h_refl != nullptr;
+        if (!p.h_refl_borrowed)
+            p.h_refl = nullptr;
         st = plan_reserve_refl(&p, n_refl);
+    }
     if (!st && !ib_cls)
         st = plan_default_config(&p);
     if (!st) {

@@ -1535,6 +1535,20 @@ int gridding_map_occupancy(int *blocks_per_sm)
 
 int absorption_block_threads() { return kBlock; }
 
+// Preferred shared-memory carveout (percent of the unified L1/shared storage)
+// of every absorption kernel; a hint to the driver.
+int absorption_set_carveout(int pct)
+{
+    cudaError_t e = cudaSuccess;
+#define ANACOR_CARVE(B, F) \
+    if (e == cudaSuccess) \
+        e = cudaFuncSetAttribute(absorption_kernel<B, F>, cudaFuncAttributePreferredSharedMemoryCarveout, pct)
+    ANACOR_CARVE(1, false); ANACOR_CARVE(2, false); ANACOR_CARVE(3, false); ANACOR_CARVE(4, false);
+    ANACOR_CARVE(1, true); ANACOR_CARVE(2, true); ANACOR_CARVE(3, true); ANACOR_CARVE(4, true);
+#undef ANACOR_CARVE
+    return e == cudaSuccess ? kOk : kErrCuda;
+}
+
 int absorption_occupancy(int *blocks_per_sm, int variant)
 {
     cudaError_t e;

@@ -95,6 +95,7 @@ int plan_view(const anacor_plan *p, PlanView *out);
 
 int rcp_table_init();
 int absorption_block_threads();
+int absorption_set_carveout(int pct);
 // Kernel variants: 1..4 the cooperative march with a register budget for
 // 1..4 CTAs per SM; 5..8 the same budgets with the distance-field march
 // (every sample needs its `field`).

@@ -823,7 +823,7 @@ int plan_default_config(anacor_plan *p)
     int variant = 0;
     const int big = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
     if (!std::getenv("ANACOR_CTAS_PER_SM") && big >= 256) {
-        // the octant fields take 5x longer to build than the centred one and
+        // the octant fields take 3x longer to build than the centred one and
         // march 15-25 % faster: worth it once the run covers twice the volume
         const long long nvol = (long long)p->dims[0] * p->dims[1] * p->dims[2];
         const int kind = p->n_refl * (long long)p->n_vox >= 2 * nvol ? 2 : 1;

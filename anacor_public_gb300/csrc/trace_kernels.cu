@@ -514,8 +514,8 @@ struct LegState {
 };
 
 // cube_face and the march set-up of one leg (warp-synchronous).  With kField
-// the field march runs here when kMarchNow, else the caller runs it.
-template <bool kDetail, bool kField, bool kMarchNow>
+// the lane's field march runs here too.
+template <bool kDetail, bool kField>
 __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx, bool valid,
                                           const Vol &v, int full, uint16_t *seg, LegResult &out, LegState &S)
 {
@@ -582,8 +582,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
             base = g.cs * g.Ss + g.ca * g.Sa + g.cb * g.Sb;
             seg[0] = (uint16_t)(3 << 13);
             if (kField) {
-                // per lane, no warp synchronisation: the field march (now, or
-                // by the caller together with the other leg)
+                // per lane, no warp synchronisation: the field march
                 const uint8_t *fld = v.field + R.octant * v.field_stride;
                 b0 = __ldg(fld + base);
                 if ((b0 & 7u) == 0) {
@@ -591,7 +590,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
                 } else {
                     m.prev = (int)(b0 & 7u);
                     live = lim > 1;
-                    if (kMarchNow && live)
+                    if (live)
                         field_march(R, g, cz, cy, cx, v, fld, base, lim, b0, m, stopped, seg);
                 }
             } else {
@@ -617,7 +616,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
     S.b0 = b0;
 }
 
-// The warp-cooperative march of the legs set up by leg_setup<.., false, ..>.
+// The warp-cooperative march of the legs set up by leg_setup<.., false>.
 __device__ __forceinline__ void leg_coop(const FaceRule *rules, int cz, int cy, int cx, const Vol &v, uint16_t *seg,
                                          LegState &S)
 {
@@ -889,7 +888,7 @@ __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rule
                                           LegResult &out, const float *voxelf = nullptr)
 {
     LegState S;
-    leg_setup<kDetail, kField, true>(h, rules, cz, cy, cx, valid, v, full, seg, out, S);
+    leg_setup<kDetail, kField>(h, rules, cz, cy, cx, valid, v, full, seg, out, S);
     if (!kField)
         leg_coop(rules, cz, cy, cx, v, seg, S);
     leg_finish<kDetail, kF32>(rules, cz, cy, cx, v, full, voxel, sq, sq_stride, qtab, seg, S, out, voxelf);

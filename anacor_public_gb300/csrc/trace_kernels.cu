@@ -444,15 +444,21 @@ __device__ __forceinline__ void chain_done(const FieldChain &c, March &m)
     m.nseg = c.nseg;
 }
 
+// The march of one lane on its field.  dlast: |displacement| of the last
+// accepted increment on the two non-step axes (a | b << 16), when its
+// fixed-point position is not near a rounding boundary; else -1.
 __device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx,
                                             const Vol &v, const uint8_t *fld, int base, int lim, uint32_t b0,
-                                            March &m, bool &stopped, uint16_t *seg)
+                                            March &m, bool &stopped, uint16_t *seg, int &dlast)
 {
     FieldChain c;
     chain_init(c, R, g, fld, base, lim, b0, m);
     while (c.on)
         chain_step(c, chain_load(c, cz, cy, cx, v), seg, stopped);
     chain_done(c, m);
+    const long long ea = c.off + (long long)c.last * c.Qa, eb = c.off + (long long)c.last * c.Qb;
+    const bool amb = ((uint32_t)ea + c.Ma < 2u * c.Ma) | ((uint32_t)eb + c.Mb < 2u * c.Mb);
+    dlast = amb ? -1 : (abs((int)(ea >> 32)) | abs((int)(eb >> 32)) << 16);
 }
 
 // fl(fl(d * v_axis)^2), from the sample's table when it has one
@@ -505,12 +511,41 @@ struct LegResult {
 };
 
 
+// cal_path2_plus in FP32 for A_h: total = |(dz, dy, dx) * voxel| (y, z, x
+// order) and tot * (span / (len - 1)) per class segment of the shared buffer.
+__device__ __forceinline__ void lengths_f32(int dz, int dy, int dx, int len, int nseg, const uint16_t *seg,
+                                            const double *voxel, const float *voxelf, LegResult &out)
+{
+    const float vy = voxelf ? voxelf[1] : (float)voxel[1];
+    const float vz = voxelf ? voxelf[0] : (float)voxel[0];
+    const float vx = voxelf ? voxelf[2] : (float)voxel[2];
+    const float ty = __fmul_rn((float)dy, vy);
+    const float tz = __fmul_rn((float)dz, vz);
+    const float tx = __fmul_rn((float)dx, vx);
+    const float totf = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ty, ty), __fmul_rn(tz, tz)), __fmul_rn(tx, tx)));
+    const float scale = __fdiv_rn(totf, (float)(len - 1));
+    int cur = seg[0];
+    for (int j = 0; j < nseg; j++) {
+        const int nxt = (j + 1 < nseg) ? (int)seg[(j + 1) * kBlock] : -1;
+        const int start = cur & 0x1fff;
+        const int end = (j + 1 < nseg) ? (nxt & 0x1fff) : len;
+        const int cls = cur >> 13;
+        const float term = scale * (float)(end - start);
+        out.Lf[0] += cls == 1 ? term : 0.0f;
+        out.Lf[1] += cls == 2 ? term : 0.0f;
+        out.Lf[2] += cls == 3 ? term : 0.0f;
+        out.Lf[3] += cls == 4 ? term : 0.0f;
+        cur = nxt;
+    }
+}
+
 // State of one leg between its set-up, its march and its lengths.
 struct LegState {
     March m;
     int face, lim, base;
     bool need, coop, stopped, live;
     uint32_t b0;   // field byte of increment 0 (field march)
+    int dlast;     // field march: the last point's displacement (see field_march), else -1
 };
 
 // cube_face and the march set-up of one leg (warp-synchronous).  With kField
@@ -545,6 +580,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
     bool coop = false, stopped = false, live = false;
     int lim = 0, base = 0;
     uint32_t b0 = 0;
+    int dlast = -1;
     if (need) {
         const FaceRule &R = rules[face - 1];
         LegGeom g;
@@ -591,7 +627,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
                     m.prev = (int)(b0 & 7u);
                     live = lim > 1;
                     if (live)
-                        field_march(R, g, cz, cy, cx, v, fld, base, lim, b0, m, stopped, seg);
+                        field_march(R, g, cz, cy, cx, v, fld, base, lim, b0, m, stopped, seg, dlast);
                 }
             } else {
                 const int lab0 = __ldg(v.p + base);
@@ -614,6 +650,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
     S.stopped = stopped;
     S.live = live;
     S.b0 = b0;
+    S.dlast = dlast;
 }
 
 // The warp-cooperative march of the legs set up by leg_setup<.., false>.
@@ -746,6 +783,24 @@ __device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy
     if (!need)
         return;
 
+    if (kF32 && coop && stopped && S.dlast >= 0 && m.nseg <= kMaxSegments) {
+        // a field march that stopped at vacuum: the last point is known
+        // (step axis: last_i increments; the others: dlast), so the lengths
+        // need neither the geometry nor the point
+        const int len = m.last_i + 1;
+        out.len = len;
+        out.nseg = m.nseg;
+        if (len == 1)
+            return;
+        const int s = rules[face - 1].count_axis;
+        const int da = S.dlast & 0xffff, db = S.dlast >> 16;
+        const int d0 = s == 0 ? m.last_i : da;
+        const int d1 = s == 1 ? m.last_i : (s == 0 ? da : db);
+        const int d2 = s == 2 ? m.last_i : db;
+        lengths_f32(d0, d1, d2, len, m.nseg, seg, voxel, voxelf, out);
+        return;
+    }
+
     // ---- after the march: geometry again, the per-lane paths, lengths
     const FaceRule &R = rules[face - 1];
     LegGeom g;
@@ -796,28 +851,7 @@ __device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy
             return;
     }
     if (kF32 && m.nseg <= kMaxSegments) {
-        // total and segment fractions in FP32: tot * (span / (len - 1))
-        const float vy = voxelf ? voxelf[1] : (float)voxel[1];
-        const float vz = voxelf ? voxelf[0] : (float)voxel[0];
-        const float vx = voxelf ? voxelf[2] : (float)voxel[2];
-        const float ty = __fmul_rn((float)abs(ly - fy), vy);
-        const float tz = __fmul_rn((float)abs(lz - fz), vz);
-        const float tx = __fmul_rn((float)abs(lx - fx), vx);
-        const float totf = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ty, ty), __fmul_rn(tz, tz)), __fmul_rn(tx, tx)));
-        const float scale = __fdiv_rn(totf, (float)(len - 1));
-        int cur = seg[0];
-        for (int j = 0; j < m.nseg; j++) {
-            const int nxt = (j + 1 < m.nseg) ? (int)seg[(j + 1) * kBlock] : -1;
-            const int start = cur & 0x1fff;
-            const int end = (j + 1 < m.nseg) ? (nxt & 0x1fff) : len;
-            const int cls = cur >> 13;
-            const float term = scale * (float)(end - start);
-            out.Lf[0] += cls == 1 ? term : 0.0f;
-            out.Lf[1] += cls == 2 ? term : 0.0f;
-            out.Lf[2] += cls == 3 ? term : 0.0f;
-            out.Lf[3] += cls == 4 ? term : 0.0f;
-            cur = nxt;
-        }
+        lengths_f32(abs(lz - fz), abs(ly - fy), abs(lx - fx), len, m.nseg, seg, voxel, voxelf, out);
         return;
     }
     if (kF32) {

@@ -767,6 +767,18 @@ __device__ __forceinline__ void leg_coop(const FaceRule *rules, int cz, int cy, 
     }
     S.m = m;
     S.stopped = stopped;
+    if (coop && stopped) {
+        // the last point of a leg that stopped at vacuum, as the field march
+        // gives it (see field_march's dlast)
+        const FaceRule &R = rules[face - 1];
+        const int s = R.count_axis, a = s == 0 ? 1 : 0, b = s == 2 ? 1 : 2;
+        const long long off = R.use_round ? 0x80000000ll : 0ll;
+        const uint32_t Ma = ((R.exact_mask >> a) & 1) ? 0u : kAmbiguityMargin;
+        const uint32_t Mb = ((R.exact_mask >> b) & 1) ? 0u : kAmbiguityMargin;
+        const long long ea = off + (long long)m.last_i * R.Q[a], eb = off + (long long)m.last_i * R.Q[b];
+        const bool amb = ((uint32_t)ea + Ma < 2u * Ma) | ((uint32_t)eb + Mb < 2u * Mb);
+        S.dlast = amb ? -1 : (abs((int)(ea >> 32)) | abs((int)(eb >> 32)) << 16);
+    }
 }
 
 // After the march: the per-lane remainder of the path and cal_path2_plus.

@@ -137,8 +137,12 @@ class Plan:
         return int(n.value)
 
     def configure(self, variant: int = 0, tile: int = 0, order: int = -1):
-        """Execution parameters: kernel register-budget variant (CTAs/SM), voxels
-        per work item, voxel order (0 the caller's, 1 Morton, 2..7 blocked)."""
+        """Execution parameters.  variant: 1..4 the warp-cooperative march
+        compiled for 1..4 CTAs per SM, 5..8 the march on the chessboard distance
+        field, 9..12 on the 8 octant fields (both need labels in 0..7), 0 the
+        process default; tile: voxels per work item (0 unchanged); order: voxel
+        order (0 the caller's, 1 Morton, 2..7 blocked, -1 unchanged).  Results
+        do not depend on them beyond the FP32 summation order of A_h."""
         _lib.check(self._L.anacor_plan_configure(self._h, int(variant), int(tile), int(order)), self._L)
 
     def config(self) -> dict:

@@ -962,6 +962,19 @@ int batch_check(anacor_batch *b, cudaStream_t st)
 }  // namespace
 
 namespace anacor {
+int plan_view_field(anacor_plan *p, PlanView *v)
+{
+    if (int st = plan_view(p, v))
+        return st;
+    if (plan_ensure_field(p, 2) == kOk) {
+        v->field = p->d_field8;
+        v->field_stride = (long long)p->dims[0] * p->dims[1] * p->dims[2];
+    } else {
+        succeed();   // labels outside 0..7: the cooperative march
+    }
+    return kOk;
+}
+
 int plan_view(const anacor_plan *p, PlanView *v)
 {
     if (!p || !v)

@@ -292,12 +292,15 @@ int run_map(const PlanView &pv, const ReflTable *d_dirs, long long n_dirs, int i
     d.sq = pv.sq;
     d.sq_stride = pv.sq_stride;
     d.qtab = pv.qtab;
+    d.field = pv.field;
+    d.field_stride = pv.field_stride;
     cudaError_t e;
     if ((e = cudaMemsetAsync(d_status, 0, sizeof(int), st)) ||
         (e = cudaMemcpyAsync(d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, st)))
         return cuda_err(e);
     const long long items = n_dirs * d.tiles;
-    if ((e = launch_gridding_map(d_desc, items, d_counter, (int)std::max(1ll, std::min<long long>(items, grid)), st)))
+    if ((e = launch_gridding_map(d_desc, items, d_counter, (int)std::max(1ll, std::min<long long>(items, grid)), st,
+                                 pv.field != nullptr)))
         return cuda_err(e);
     // the descriptor is on the stack
     return check_map_status(d_status, st);
@@ -337,7 +340,8 @@ anacor_gridding *anacor_gridding_create(anacor_plan *plan, int n_theta, int n_ph
         return nullptr;
     }
     g->plan = plan;
-    if (plan_view(plan, &g->pv)) {
+    // the map marches every voxel in every grid direction: on the octant fields
+    if (plan_view_field(plan, &g->pv)) {
         delete g;
         return nullptr;
     }

@@ -1316,6 +1316,7 @@ __global__ void __launch_bounds__(kBlock, 2) bisection_kernel(const SampleDesc *
 
 // Absorption map: work item = (grid direction, tile of voxels); the
 // diffracted leg of every voxel, one output per (direction, voxel).
+template <bool kField>
 __global__ void __launch_bounds__(kBlock, 2) gridding_map_kernel(const MapDesc *__restrict__ dp, long long total_items,
                                                                  unsigned long long *__restrict__ work_counter)
 {
@@ -1324,7 +1325,7 @@ __global__ void __launch_bounds__(kBlock, 2) gridding_map_kernel(const MapDesc *
     __shared__ long long item_s;
     const MapDesc &D = *dp;
     const int tid = threadIdx.x;
-    const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2]};
+    const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field, D.field_stride};
     for (;;) {
         if (tid == 0)
             item_s = (long long)atomicAdd(work_counter, 1ull);
@@ -1350,8 +1351,8 @@ __global__ void __launch_bounds__(kBlock, 2) gridding_map_kernel(const MapDesc *
             const bool valid = vi < v1;
             const short4 cv = valid ? __ldg(D.coords + vi) : make_short4(0, 0, 0, 0);
             LegResult a;
-            trace_leg<false>(tab.head[1], tab.rule[1], cv.x, cv.y, cv.z, valid, v, D.full_iteration, D.voxel,
-                             D.sq, D.sq_stride, D.qtab, seg + tid, a);
+            trace_leg<false, false, kField>(tab.head[1], tab.rule[1], cv.x, cv.y, cv.z, valid, v, D.full_iteration,
+                                            D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a);
             if (!valid)
                 continue;
             double val;
@@ -1560,22 +1561,27 @@ int bisection_occupancy(int *blocks_per_sm)
 }
 
 cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,
-                                cudaStream_t st)
+                                cudaStream_t st, bool field)
 {
     if (total_items <= 0)
         return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess)
         return e;
-    gridding_map_kernel<<<grid, kBlock, 0, st>>>(d_desc, total_items, d_counter);
+    if (field)
+        gridding_map_kernel<true><<<grid, kBlock, 0, st>>>(d_desc, total_items, d_counter);
+    else
+        gridding_map_kernel<false><<<grid, kBlock, 0, st>>>(d_desc, total_items, d_counter);
     return cudaGetLastError();
 }
 
-int gridding_map_occupancy(int *blocks_per_sm)
+int gridding_map_occupancy(int *blocks_per_sm, bool field)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gridding_map_kernel, kBlock, 0) == cudaSuccess
-               ? kOk
-               : kErrCuda;
+    const cudaError_t e = field ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gridding_map_kernel<true>,
+                                                                                kBlock, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gridding_map_kernel<false>,
+                                                                                kBlock, 0);
+    return e == cudaSuccess ? kOk : kErrCuda;
 }
 
 int absorption_block_threads() { return kBlock; }

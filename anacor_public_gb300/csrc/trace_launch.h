@@ -73,6 +73,8 @@ struct MapDesc {
     const double *sq;
     int sq_stride;
     const double *qtab;
+    const uint8_t *field;   // optional: octant fields (launch_octant_fields) for the field march
+    long long field_stride;
 };
 
 // Device-resident sample of a plan, for the other entry points that march it.
@@ -90,8 +92,13 @@ struct PlanView {
     const double *qtab;
     cudaStream_t stream;
     int sms;
+    const uint8_t *field;     // the plan's octant fields, when built (plan_view_field)
+    long long field_stride;
 };
 int plan_view(const anacor_plan *p, PlanView *out);
+// plan_view with the plan's octant fields, built if needed (left out, with
+// no error, when the labels do not fit 3 bits)
+int plan_view_field(anacor_plan *p, PlanView *out);
 
 int rcp_table_init();
 int absorption_block_threads();
@@ -150,8 +157,8 @@ cudaError_t launch_bisection(const SampleDesc *d_descs, int n_desc, long long to
 int bisection_occupancy(int *blocks_per_sm);
 // Persistent launch over n_dirs * tiles work items of the map.
 cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,
-                                cudaStream_t st);
-int gridding_map_occupancy(int *blocks_per_sm);
+                                cudaStream_t st, bool field = false);
+int gridding_map_occupancy(int *blocks_per_sm, bool field = false);
 // Lookup of one reflection in an absorption map: for each leg (0 incident,
 // 1 diffracted) the map rows (grid directions) and weights of the value, as
 // the reference's interpolation reads it

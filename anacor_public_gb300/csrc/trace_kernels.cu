@@ -539,6 +539,31 @@ __device__ __forceinline__ void lengths_f32(int dz, int dy, int dx, int len, int
     }
 }
 
+// cal_path2_plus in FP64, bit for bit as the reference: total from the
+// squares fl(fl(d * voxel)^2) summed y, z, x, then tot * fl(span / (len - 1))
+// per class segment of the shared buffer, added in segment order.
+__device__ __forceinline__ void lengths_f64(int dz, int dy, int dx, int len, int nseg, const uint16_t *seg,
+                                            const double *voxel, const double *sq, int sq_stride, const double *qtab,
+                                            LegResult &out)
+{
+    const double yy = sq_len(sq, sq_stride, 1, dy, voxel[1]);
+    const double zz = sq_len(sq, sq_stride, 0, dz, voxel[0]);
+    const double xx = sq_len(sq, sq_stride, 2, dx, voxel[2]);
+    const double tot = __dsqrt_rn(__dadd_rn(__dadd_rn(yy, zz), xx));
+    const int den_i = len - 1;
+    const double2 dr = g_num_rcp[den_i];
+    int seen = 0;
+    int cur = seg[0];
+    for (int j = 0; j < nseg; j++) {
+        const int nxt = (j + 1 < nseg) ? (int)seg[(j + 1) * kBlock] : -1;
+        const int start = cur & 0x1fff;
+        const int end = (j + 1 < nseg) ? (nxt & 0x1fff) : len;
+        const double q = seg_quotient(qtab, den_i, end - start, dr.x, dr.y);
+        add_class(cur >> 13, __dmul_rn(tot, q), seen, out.L);
+        cur = nxt;
+    }
+}
+
 // State of one leg between its set-up, its march and its lengths.
 struct LegState {
     March m;
@@ -795,7 +820,7 @@ __device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy
     if (!need)
         return;
 
-    if (kF32 && coop && stopped && S.dlast >= 0 && m.nseg <= kMaxSegments) {
+    if (!kDetail && coop && stopped && S.dlast >= 0 && m.nseg <= kMaxSegments) {
         // a field march that stopped at vacuum: the last point is known
         // (step axis: last_i increments; the others: dlast), so the lengths
         // need neither the geometry nor the point
@@ -809,7 +834,10 @@ __device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy
         const int d0 = s == 0 ? m.last_i : da;
         const int d1 = s == 1 ? m.last_i : (s == 0 ? da : db);
         const int d2 = s == 2 ? m.last_i : db;
-        lengths_f32(d0, d1, d2, len, m.nseg, seg, voxel, voxelf, out);
+        if (kF32)
+            lengths_f32(d0, d1, d2, len, m.nseg, seg, voxel, voxelf, out);
+        else
+            lengths_f64(d0, d1, d2, len, m.nseg, seg, voxel, sq, sq_stride, qtab, out);
         return;
     }
 
@@ -873,25 +901,16 @@ __device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy
             out.Lf[k] = (float)r.v[k];
         return;
     }
-    // total from the first and last path points, y then z then x
-    const double yy = sq_len(sq, sq_stride, 1, abs(ly - fy), voxel[1]);
-    const double zz = sq_len(sq, sq_stride, 0, abs(lz - fz), voxel[0]);
-    const double xx = sq_len(sq, sq_stride, 2, abs(lx - fx), voxel[2]);
-    const double tot = __dsqrt_rn(__dadd_rn(__dadd_rn(yy, zz), xx));
-    const int den_i = len - 1;
-    const double2 dr = g_num_rcp[den_i];
-    int seen = 0;
     if (m.nseg <= kMaxSegments) {
-        int cur = seg[0];
-        for (int j = 0; j < m.nseg; j++) {
-            const int nxt = (j + 1 < m.nseg) ? (int)seg[(j + 1) * kBlock] : -1;
-            const int start = cur & 0x1fff;
-            const int end = (j + 1 < m.nseg) ? (nxt & 0x1fff) : len;
-            const double q = seg_quotient(qtab, den_i, end - start, dr.x, dr.y);
-            add_class(cur >> 13, __dmul_rn(tot, q), seen, out.L);
-            cur = nxt;
-        }
+        lengths_f64(abs(lz - fz), abs(ly - fy), abs(lx - fx), len, m.nseg, seg, voxel, sq, sq_stride, qtab, out);
     } else {
+        // total from the first and last path points, y then z then x
+        const double yy = sq_len(sq, sq_stride, 1, abs(ly - fy), voxel[1]);
+        const double zz = sq_len(sq, sq_stride, 0, abs(lz - fz), voxel[0]);
+        const double xx = sq_len(sq, sq_stride, 2, abs(lx - fx), voxel[2]);
+        const double tot = __dsqrt_rn(__dadd_rn(__dadd_rn(yy, zz), xx));
+        const int den_i = len - 1;
+        const double2 dr = g_num_rcp[den_i];
         // more class changes than the shared buffer holds: march again and
         // accumulate as segments close (same terms, same order)
         March m2;

@@ -24,6 +24,10 @@ Fixtures (all small):
                     ray_tracing_single, beside the analytic transmission values
                     that AnACor/verification/sphere_verification_new.py:31-36
                     checks against.
+  cylinder_kat.npz  the same for a voxelised cylinder (axis along the
+                    volume's first axis, rays perpendicular to it) against the
+                    values AnACor/verification/cylinder_verification_new.py:31-33
+                    checks against (python make_golden.py --cylinder).
 """
 from __future__ import annotations
 
@@ -53,6 +57,20 @@ SPHERE_ANALYTIC = {
 SPHERE_RADIUS = 24          # voxels
 SPHERE_VOXEL = 0.5          # um
 
+# analytic cylinder transmission factors at 2theta = linspace(0, 180, 10),
+# rays perpendicular to the axis (AnACor/verification/cylinder_verification_new.py:31-33)
+CYLINDER_ANALYTIC = {
+    0.1: [0.84438065, 0.84445195, 0.84473729, 0.84516565, 0.84580902,
+          0.84652501, 0.84731401, 0.84796065, 0.8483923, 0.84853627],
+    0.5: [0.43485824, 0.43618599, 0.44012147, 0.44646843, 0.45462811,
+          0.46373586, 0.47276853, 0.4805613, 0.48593226, 0.48787627],
+    1.0: [0.19643664, 0.19926273, 0.2074861, 0.22007527, 0.23551023,
+          0.25211779, 0.26819718, 0.28199199, 0.29158769, 0.29510712],
+}
+CYLINDER_RADIUS = 24        # voxels
+CYLINDER_LENGTH = 2         # voxels along the axis (rays never move along it)
+CYLINDER_VOXEL = 0.5        # um
+
 
 def digest(*arrays) -> str:
     h = hashlib.sha256()
@@ -75,6 +93,49 @@ def sphere_volume(radius: int):
     zz, yy, xx = np.meshgrid(g, g, g, indexing="ij", sparse=True)
     vol = np.where(zz ** 2 + yy ** 2 + xx ** 2 < radius ** 2, 3, 0).astype(np.int8)
     return np.ascontiguousarray(vol)
+
+
+def cylinder_volume(radius: int, length: int):
+    """Crystal (label 3) cylinder of `radius` voxels whose axis runs along the
+    volume's first axis, in a (length, 3r, 3r) volume."""
+    n = 3 * radius
+    c = n / 2 - 1
+    g = np.arange(n, dtype=np.float64) - c
+    yy, xx = np.meshgrid(g, g, indexing="ij")
+    disc = np.where(yy ** 2 + xx ** 2 < radius ** 2, 3, 0).astype(np.int8)
+    return np.ascontiguousarray(np.repeat(disc[None, :, :], length, axis=0))
+
+
+def cylinder_directions(two_theta_deg):
+    """Rotated incident / diffracted vectors at scattering angle 2theta, both
+    perpendicular to the cylinder axis: the volume's first axis is the DIALS
+    x component (the march frame swaps DIALS y and z), so both lie in the
+    DIALS y-z plane, at a generic angle to its axes."""
+    a0 = 0.37
+    out = []
+    for t in np.deg2rad(two_theta_deg):
+        b = np.array([0.0, np.cos(a0), np.sin(a0)])
+        s = np.array([0.0, np.cos(a0 + t), np.sin(a0 + t)])
+        out.append((b, s))
+    return out
+
+
+def cylinder_kat(ref):
+    vol = cylinder_volume(CYLINDER_RADIUS, CYLINDER_LENGTH)
+    coords = np.ascontiguousarray(np.argwhere(vol == 3).astype(np.int64))[::5]
+    tth = np.linspace(0, 180, 10)
+    voxel = np.array([CYLINDER_VOXEL] * 3)
+    res = {}
+    for mur in (0.1, 0.5, 1.0):
+        mu = np.array([0.0, 0.0, mur / (CYLINDER_RADIUS * CYLINDER_VOXEL), 0.0])
+        res[mur] = [ref.single(coords, sr, xr, voxel, mu, vol) for xr, sr in cylinder_directions(tth)]
+    np.savez_compressed(os.path.join(HERE, "cylinder_kat.npz"), coords=coords, two_theta=tth,
+                        mur=np.array([0.1, 0.5, 1.0]),
+                        reference=np.array([res[m] for m in (0.1, 0.5, 1.0)]),
+                        analytic=np.array([CYLINDER_ANALYTIC[m] for m in (0.1, 0.5, 1.0)]))
+    for m in (0.1, 0.5, 1.0):
+        err = np.abs(np.array(res[m]) - CYLINDER_ANALYTIC[m]) / np.array(CYLINDER_ANALYTIC[m])
+        print("cylinder mu*r", m, "max rel err vs analytic", err.max())
 
 
 def sphere_directions(two_theta_deg):
@@ -124,6 +185,9 @@ def main():
     if "--modes" in sys.argv:
         bisection_and_gridding(ref)
         return
+    if "--cylinder" in sys.argv:
+        cylinder_kat(ref)
+        return
 
     s = synth.small_sample()
     ah = ref.overall(s, num_workers=os.cpu_count() or 1)
@@ -162,6 +226,7 @@ def main():
         err = np.abs(np.array(res[m]) - SPHERE_ANALYTIC[m]) / np.array(SPHERE_ANALYTIC[m])
         print("sphere mu*r", m, "max rel err vs analytic", err.max())
     bisection_and_gridding(ref)
+    cylinder_kat(ref)
 
 
 if __name__ == "__main__":

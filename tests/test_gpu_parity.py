@@ -263,3 +263,27 @@ def test_batch_of_samples_one_launch(lib, oracle):
     for s, p in zip(samples, plans):
         assert max_rel(p.result(), oracle.overall(s, threads=os.cpu_count() or 1)) <= RTOL
         p.close()
+
+
+@pytest.mark.parametrize("shape", ["sphere", "cylinder"])
+def test_known_answer_volumes(lib, golden_dir, shape):
+    """The analytic sphere and cylinder sets (reference values and analytic
+    transmission factors in tests/golden): ray_tracing_single on the GPU gives
+    the reference's A_h within 1e-6 for every mu*r and 2theta."""
+    from tests.golden.make_golden import cylinder_directions, cylinder_volume, sphere_directions, sphere_volume
+    g = np.load(os.path.join(golden_dir, f"{shape}_kat.npz"))
+    if shape == "sphere":
+        vol, dirs = sphere_volume(24), sphere_directions(g["two_theta"])
+    else:
+        vol, dirs = cylinder_volume(24, 2), cylinder_directions(g["two_theta"])
+    tab, keep = row_table(vol)
+    voxel = np.array([0.5] * 3)
+    coords = np.ascontiguousarray(g["coords"])
+    for k, mur in enumerate(g["mur"]):
+        mu = np.array([0.0, 0.0, mur / (24 * 0.5), 0.0])
+        for j, (xr, sr) in enumerate(dirs):
+            got = lib.ray_tracing_single(coords, len(coords), np.ascontiguousarray(sr), np.ascontiguousarray(xr),
+                                         voxel, mu, tab, np.array(vol.shape, dtype=np.int64), 0, 0, 1)
+            want = g["reference"][k][j]
+            assert abs(got - want) <= RTOL * want, (shape, mur, j, got, want)
+    del keep

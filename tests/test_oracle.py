@@ -7,7 +7,8 @@ import pytest
 
 from anacor_public_gb300 import synth
 from oracle import oracle as orc
-from tests.golden.make_golden import sample_digest, sphere_directions, sphere_volume
+from tests.golden.make_golden import (cylinder_directions, cylinder_volume, sample_digest, sphere_directions,
+                                      sphere_volume)
 
 
 def test_generator_reproduces_golden_inputs(small, golden_dir):
@@ -48,6 +49,20 @@ def test_oracle_sphere_known_answers(oracle, golden_dir):
     voxel = np.array([0.5] * 3)
     dirs = sphere_directions(g["two_theta"])
     # discretisation error of the reference's method grows with mu*r
+    tol = {0.1: 0.01, 0.5: 0.04, 1.0: 0.07}
+    for k, mur in enumerate(g["mur"]):
+        mu = np.array([0.0, 0.0, mur / (24 * 0.5), 0.0])
+        got = np.array([oracle.single(g["coords"], sr, xr, voxel, mu, vol) for xr, sr in dirs])
+        assert np.array_equal(got, g["reference"][k])
+        rel = np.abs(got - g["analytic"][k]) / g["analytic"][k]
+        assert rel.max() < tol[float(mur)]
+
+
+def test_oracle_cylinder_known_answers(oracle, golden_dir):
+    g = np.load(os.path.join(golden_dir, "cylinder_kat.npz"))
+    vol = cylinder_volume(24, 2)
+    voxel = np.array([0.5] * 3)
+    dirs = cylinder_directions(g["two_theta"])
     tol = {0.1: 0.01, 0.5: 0.04, 1.0: 0.07}
     for k, mur in enumerate(g["mur"]):
         mu = np.array([0.0, 0.0, mur / (24 * 0.5), 0.0])

@@ -21,12 +21,18 @@
 //              boundary are recomputed with the reference's FP64 expression.
 //              Lanes that may touch a volume wall, faces with ratios beyond
 //              fixed-point range and full_iteration march per lane in FP64.
+//              Field variants: each lane marches alone on a packed label +
+//              chessboard-distance field (centred, or one per direction
+//              octant) and steps over the increments the field proves to keep
+//              their label; stops, class changes and len_path_2 are those of
+//              the per-increment march.
 //   lengths    (cal_path2_plus, :1462-1552): for A_h in FP32 (the segments and
 //              len_path_2 come from the exact march; A_h needs 1e-6); for the
 //              per-voxel detail and the gridding map in FP64 with the
 //              reference's operation order, the per-segment quotient
 //              fl(span / (len-1)) from a table of correctly rounded quotients,
-//              or a correctly rounded reciprocal and one FMA correction.
+//              or a correctly rounded reciprocal and one FMA correction.  A
+//              leg that stopped at vacuum takes its last point from the march.
 //   rate       (cal_rate, :1554-1583): FP32 exponent and exp; per-thread
 //              Neumaier sums, warp-shuffle TwoSum reduction, tile partials
 //              combined in FP64 in a fixed order (deterministic for any
@@ -52,8 +58,9 @@ namespace {
 constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
 // CTAs per SM the absorption kernel's register budget is sized for: the
-// kernel is instantiated for 1..4 and one variant is chosen per process
-// (ANACOR_CTAS_PER_SM, default kDefaultMinBlocks).
+// kernel is instantiated for 1..4 (times the two marches); the plan's
+// variant, or the process default (ANACOR_CTAS_PER_SM, default
+// kDefaultMinBlocks), picks one.
 constexpr int kDefaultMinBlocks = 4;
 // Label loads a lane has in flight before checking them (divides 32).
 constexpr int kMarchBatch = 8;

@@ -1510,6 +1510,21 @@ int anacor_rotated_vectors(const double *omega_axis, const double *omega, const 
     return succeed();
 }
 
+int anacor_block_guard_check(int threads, int32_t *status)
+{
+    DeviceState *d = nullptr;
+    if (int st = current_device(&d))
+        return st;
+    int word = 0;
+    const int st = block_guard_selftest(threads, &word);
+    if (st)
+        return fail(st, st == kErrArgs ? "threads must be a positive multiple of 32, at most the block size"
+                                       : "block-guard launch failed");
+    if (status)
+        *status = word;
+    return succeed();
+}
+
 int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *coords, int64_t n,
                       const double *rotated_s1, const double *rotated_xray, const double *voxel,
                       int full_iteration, int32_t *face, int32_t *len, int32_t *nseg, int32_t *first,

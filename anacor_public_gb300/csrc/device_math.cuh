@@ -6,7 +6,12 @@
 
 namespace anacor {
 
-// exp(-x) in FP32 after an FP64 reduction x = k ln2 + r, |r| <= ln2/2.
+// exp(-x) = 2^-k exp(-r) with the additive range reduction of exp by
+// multiples of ln 2 (Cody and Waite, "Software Manual for the Elementary
+// Functions", 1980, the exp chapter): k = rint(x / ln2), r = x - k ln2 in FP64
+// (one FP64 constant instead of their two-part split: the rounding of k ln2,
+// ~1e-16 k, is far below FP32's resolution), then CUDA's expf on the FP32 r,
+// |r| <= ln2/2, and an exact scaling by 2^-k.
 __device__ __forceinline__ float exp_neg(double x)
 {
     const double kd = rint(__dmul_rn(x, 1.4426950408889634));

@@ -2,9 +2,10 @@
 // allocate device memory.
 //
 // Some callers cannot call cudaMalloc (or any allocator) at the moment they
-// need absorption factors: code running while a CUDA graph is being recorded
-// by someone else, embedded hosts whose device memory is owned by a pool they
-// do not control, or real-time pipelines that forbid allocation after start-up.
+// need absorption factors: hosts whose device memory is owned by a pool they
+// do not control (a framework allocator that has reserved the device), or
+// real-time pipelines that forbid allocation after start-up because
+// cudaMalloc and cudaFree may synchronise the whole device.
 // This entry point takes device-resident inputs and output from the caller and
 // keeps everything else the kernel needs -- packed voxel coordinates,
 // per-reflection tables, per-tile partial sums, arrival counters, the work
@@ -89,6 +90,19 @@ int cuda_error(cudaError_t e, const char *what)
     return report_status(kErrCuda, msg);
 }
 
+// Error return once work is enqueued: drain the stream first, so that no
+// kernel of this call still reads the caller's buffers or writes the scratch
+// array when the caller gets control back.
+int drained(cudaStream_t st, int status)
+{
+    cudaStreamSynchronize(st);
+    return status;
+}
+
+// Held from the first write to the scratch array until the call returns: calls
+// from several host threads run one after another.
+std::mutex g_call_mu;
+
 }  // namespace
 
 extern "C" int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *shape, const int64_t *d_coords,
@@ -128,6 +142,7 @@ extern "C" int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *s
         return report_status(kErrArgs, msg);
     }
 
+    std::lock_guard<std::mutex> call_lock(g_call_mu);
     DeviceSetup *dev = nullptr;
     if (int st = device_setup(&dev))
         return st;
@@ -146,25 +161,24 @@ extern "C" int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *s
     // the array keeps the previous call's contents: zero what must start at zero
     if ((e = cudaMemsetAsync(d_status, 0, sizeof(int), st)) ||
         (n_refl > 0 && (e = cudaMemsetAsync(d_arrive, 0, (size_t)n_refl * sizeof(unsigned), st))))
-        return cuda_error(e, "cudaMemsetAsync");
+        return drained(st, cuda_error(e, "cudaMemsetAsync"));
     if ((e = launch_pack_coords(reinterpret_cast<const long long *>(d_coords), (int)n_coords, dims, d_pack,
                                 d_status, st)))
-        return cuda_error(e, "coordinate packing");
+        return drained(st, cuda_error(e, "coordinate packing"));
 
     // reflection tables: host FP64 set-up, one thread, in chunks through a
     // static staging area (no heap, no thread pool)
-    static std::mutex stage_mu;
-    std::lock_guard<std::mutex> lk(stage_mu);
     for (int64_t r0 = 0; r0 < n_refl; r0 += kStageTables) {
         const int64_t m = std::min<int64_t>(kStageTables, n_refl - r0);
         for (int64_t k = 0; k < m; k++)
             if (setup_reflection(omega_axis, omega[r0 + k], F, xray, s1 + 3 * (r0 + k), &g_stage[k], nullptr,
                                  nullptr))
-                return report_status(kErrDirection, "anacor_absorption_noalloc: non-finite or zero direction");
+                return drained(st, report_status(kErrDirection,
+                                                 "anacor_absorption_noalloc: non-finite or zero direction"));
         if ((e = cudaMemcpyAsync(d_tables + r0, g_stage, (size_t)m * sizeof(ReflTable), cudaMemcpyHostToDevice,
                                  st)) ||
             (e = cudaStreamSynchronize(st)))
-            return cuda_error(e, "table upload");
+            return drained(st, cuda_error(e, "table upload"));
     }
 
     static SampleDesc desc;
@@ -194,19 +208,19 @@ extern "C" int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *s
     desc.steps = nullptr;
     desc.work_begin = 0;
     if ((e = cudaMemcpyAsync(d_desc, &desc, sizeof(desc), cudaMemcpyHostToDevice, st)))
-        return cuda_error(e, "descriptor upload");
+        return drained(st, cuda_error(e, "descriptor upload"));
 
     const long long items = (long long)n_refl * tiles;
     if (items > 0) {
         const long long cap = (long long)dev->sms * dev->blocks_per_sm;
         const int grid = (int)std::max(1ll, std::min(items, cap));
         if ((e = launch_absorption(d_desc, 1, items, d_counter, grid, st)))
-            return cuda_error(e, "kernel launch");
+            return drained(st, cuda_error(e, "kernel launch"));
     }
     int status = 0;
     if ((e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st)) ||
         (e = cudaStreamSynchronize(st)))
-        return cuda_error(e, "status download");
+        return drained(st, cuda_error(e, "status download"));
     for (int b = 1; b < 16; b++)
         if (status & (1 << b))
             return report_status(b, b == kErrArgs ? "anacor_absorption_noalloc: a coordinate lies outside the volume"

@@ -66,6 +66,20 @@ constexpr int kDefaultMinBlocks = 4;
 constexpr int kMarchBatch = 8;
 constexpr unsigned kAll = 0xffffffffu;
 
+// The kernels' shared arrays (per-warp tables, segment lists, lane sums) are
+// sized for kBlock threads.  A launch with any other block shape sets the
+// ANACOR_ERR_ARGS bit in `status` (from one thread) and returns before any
+// shared or global access; the test is uniform over the block, so no thread
+// is left waiting at a barrier.
+__device__ __forceinline__ bool block_shape_ok(int *status)
+{
+    if (blockDim.x == kBlock && blockDim.y == 1 && blockDim.z == 1)
+        return true;
+    if (status && threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0)
+        atomicOr(status, 1 << kErrArgs);
+    return false;
+}
+
 struct Vol {
     const int8_t *p;
     int dz, dy, dx;
@@ -1036,6 +1050,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
     __shared__ uint16_t seg[kMaxSegments * kBlock];
     __shared__ float lsum[4][kBlock];
 
+    if (!block_shape_ok(n_desc > 0 ? descs[0].status : nullptr))
+        return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     ReflTable &tab = tabs[warp];
     for (;;) {
@@ -1288,6 +1304,8 @@ __global__ void __launch_bounds__(kBlock, 2) bisection_kernel(const SampleDesc *
     __shared__ float red_s[kWarps], red_c[kWarps];
     __shared__ long long item_s;
     __shared__ int last_s;
+    if (!block_shape_ok(n_desc > 0 ? descs[0].status : nullptr))
+        return;
     const int tid = threadIdx.x;
     for (;;) {
         if (tid == 0)
@@ -1350,6 +1368,8 @@ __global__ void __launch_bounds__(kBlock, 2) gridding_map_kernel(const MapDesc *
     __shared__ uint16_t seg[kMaxSegments * kBlock];
     __shared__ long long item_s;
     const MapDesc &D = *dp;
+    if (!block_shape_ok(D.status))
+        return;
     const int tid = threadIdx.x;
     const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field, D.field_stride};
     for (;;) {
@@ -1418,6 +1438,8 @@ __global__ void __launch_bounds__(kBlock) leg_detail_kernel(const ReflTable *__r
     __shared__ ReflTable tab;
     __shared__ uint16_t seg[kMaxSegments * kBlock];
     __shared__ double vox[3];
+    if (!block_shape_ok(status))
+        return;
     {
         const int4 *src = reinterpret_cast<const int4 *>(tabp);
         int4 *dst = reinterpret_cast<int4 *>(&tab);
@@ -1611,6 +1633,38 @@ int gridding_map_occupancy(int *blocks_per_sm, bool field)
 }
 
 int absorption_block_threads() { return kBlock; }
+
+int block_guard_selftest(int threads, int *status_out)
+{
+    // Launch the absorption kernel over no work with `threads` threads per
+    // block, fewer than kBlock (a whole number of warps), and report the
+    // status word it leaves.  The guard must refuse the launch before any
+    // access; threads == kBlock must pass it and find no work.
+    if (threads <= 0 || threads > kBlock || threads % 32 != 0 || !status_out)
+        return kErrArgs;
+    SampleDesc h{};
+    SampleDesc *d = nullptr;
+    unsigned long long *counter = nullptr;
+    int *status = nullptr;
+    if (cudaMalloc(&d, sizeof(SampleDesc)) != cudaSuccess)
+        return kErrCuda;
+    int rc = kErrCuda;
+    if (cudaMalloc(&counter, sizeof(unsigned long long)) == cudaSuccess &&
+        cudaMalloc(&status, sizeof(int)) == cudaSuccess && cudaMemset(status, 0, sizeof(int)) == cudaSuccess &&
+        cudaMemset(counter, 0, sizeof(unsigned long long)) == cudaSuccess) {
+        h.status = status;
+        if (cudaMemcpy(d, &h, sizeof(h), cudaMemcpyHostToDevice) == cudaSuccess) {
+            absorption_kernel<2, false><<<2, threads>>>(d, 1, 0, counter);
+            if (cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
+                cudaMemcpy(status_out, status, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)
+                rc = kOk;
+        }
+    }
+    cudaFree(status);
+    cudaFree(counter);
+    cudaFree(d);
+    return rc;
+}
 
 // Preferred shared-memory carveout (percent of the unified L1/shared storage)
 // of every absorption kernel; a hint to the driver.

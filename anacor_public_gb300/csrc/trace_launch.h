@@ -102,6 +102,11 @@ int plan_view_field(anacor_plan *p, PlanView *out);
 
 int rcp_table_init();
 int absorption_block_threads();
+// Launch the absorption kernel over no work with `threads` (a multiple of 32,
+// at most the kernel's block size) threads per block; *status_out is the
+// status word it leaves (ANACOR_ERR_ARGS bit set when the block-shape guard
+// refused the launch).
+int block_guard_selftest(int threads, int *status_out);
 int absorption_set_carveout(int pct);
 // Kernel variants: 1..4 the cooperative march with a register budget for
 // 1..4 CTAs per SM; 5..8 the same budgets with the distance-field march

@@ -197,10 +197,11 @@ def high_absorption_sample(n_refl: int = 50000, stride: int = 1, seed: int = 4) 
 
 def batch_samples(n_samples: int = 12, seed: int = 2, refl_range=(2000, 60000),
                   dim_range=(128, 640), max_refl: int | None = None, voxel_budget: int = 60000,
-                  strides=(2, 4, 8)):
+                  strides=(2, 4, 8), only: int | None = None):
     """Independent samples with log-uniform dimensions, crystal diameters 15-40%
     of the smallest dimension, the same label recipe, mu jittered +-30% and
-    log-uniform reflection counts.
+    log-uniform reflection counts.  ``only=k`` builds sample k alone (the
+    same sample as in the full list) and returns it in a one-element list.
 
     The crystal-voxel sampling stride of each sample is the smallest of
     `strides` that keeps its voxel list within `voxel_budget` (the largest
@@ -221,6 +222,8 @@ def batch_samples(n_samples: int = 12, seed: int = 2, refl_range=(2000, 60000),
         mu = MU_BASE * rng.uniform(0.7, 1.3, size=4)
         scale = float(np.min(dims)) / 96.0
         sample_seed = int(rng.integers(1 << 30))
+        if only is not None and k != only:
+            continue
         # the loop grazes the liquor so that rays can cross liquor -> loop
         s = make_sample(shape=tuple(int(d) for d in dims), n_refl=n_refl, seed=sample_seed, mu=mu,
                         semi_axes=tuple(semi), shell=6.0 * scale,

@@ -202,9 +202,10 @@ void anacor_batch_destroy(anacor_batch *b);
 #define ANACOR_NOALLOC_SCRATCH_BYTES (32u << 20)
 
 /* No counterpart in the reference.  The absorption path for callers that must
- * not allocate device memory: code that runs while someone else records a
- * CUDA graph, hosts whose device memory belongs to a pool they do not
- * control, pipelines that forbid allocation after start-up.  The caller
+ * not allocate device memory: hosts whose device memory belongs to a pool
+ * they do not control (a framework allocator that has reserved the device),
+ * and pipelines that forbid allocation after start-up because cudaMalloc and
+ * cudaFree may synchronise the whole device.  The caller
  * passes device pointers for the C-contiguous int8 volume (d_label), the
  * int64 (z, y, x) voxel list (d_coords) and the result array (d_out,
  * n_refl doubles); s1, omega, xray, omega_axis, F, voxel, mu and shape are
@@ -217,10 +218,13 @@ void anacor_batch_destroy(anacor_batch *b);
  * over several calls).  The first call on a device looks up the array's
  * address and uploads a constant table, so make that first call before any
  * stream capture.  All calls share the one array and it keeps the previous
- * call's contents: the call clears what must start at zero itself, and calls
- * that overlap on the GPU (other streams, other threads) race on it.  Work is
- * enqueued on `stream` (a cudaStream_t); the call returns after the stream
- * has drained, with a status. */
+ * call's contents: the call clears what must start at zero itself.  Calls
+ * from several host threads of one process take a lock and run one after
+ * another; work on the array that the library cannot see (another process's
+ * calls, a replayed graph) races with a call.  Work is enqueued on `stream`
+ * (a cudaStream_t), from pageable host memory, and the call waits for that
+ * stream to drain before it returns, with a status, on success and on every
+ * error after the first enqueue. */
 int anacor_absorption_noalloc(const int8_t *d_label, const int64_t *shape, const int64_t *d_coords,
                               int64_t n_coords, const double *s1, const double *omega, int64_t n_refl,
                               const double *xray, const double *omega_axis, const double *F,
@@ -399,6 +403,14 @@ int anacor_leg_detail(const int8_t *label, const int64_t *shape, const int64_t *
                       const double *rotated_s1, const double *rotated_xray, const double *voxel,
                       int full_iteration, int32_t *face, int32_t *len, int32_t *nseg, int32_t *first,
                       int32_t *last, double *L, int32_t *status);
+
+/* The absorption kernel's shared arrays are sized for its fixed block of 256
+ * threads, and the kernels refuse any other block shape on the device (status
+ * bit 1 << ANACOR_ERR_ARGS, no access).  This launches the absorption kernel
+ * over no work with `threads` threads per block (a multiple of 32, at most
+ * 256) and returns the status word it left in *status: the guard bit for
+ * fewer than 256 threads, 0 for 256. */
+int anacor_block_guard_check(int threads, int32_t *status);
 
 #ifdef __cplusplus
 }

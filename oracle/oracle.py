@@ -30,9 +30,12 @@ _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 STATUS = {0: "ok", 1: "no exit face", 2: "face/angle assert", 3: "bad arguments", 4: "out of memory"}
 
 
-def build_oracle(ref: bool = False) -> None:
-    target = ["ref"] if ref else []
-    subprocess.run(["make", "-s", "-C", HERE] + target, check=True)
+def build_oracle(ref_src: str | None = None) -> None:
+    """Build the C restatement; with ``ref_src`` (the reference checkout's
+    ``AnACor/src`` directory) also the reference library from its sources."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref_src:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFSRC={os.path.abspath(ref_src)}"], check=True)
 
 
 def _c(a, dt):

@@ -28,6 +28,19 @@ Fixtures (all small):
                     volume's first axis, rays perpendicular to it) against the
                     values AnACor/verification/cylinder_verification_new.py:31-33
                     checks against (python make_golden.py --cylinder).
+
+Fixtures at the large workloads (python make_golden.py --large; the volumes
+are regenerated from their seeds by the tests, the digests pin them):
+  beamline_ah256.npz  A_h of 256 reflections of the 20,000-reflection beamline
+                      workload (512x512x400, stride-4 voxels), every voxel.
+  highabs_ah.npz      the 1024x1024x800 mu x5 workload (50,000 reflections):
+                      A_h of 48 seeded reflections over a seeded 32,768-voxel
+                      subset, and the per-voxel, per-leg detail of 2 of them
+                      on 2,048 voxels of that subset.
+  batch_ah.npz        the largest-volume sample of the 12-sample batch
+                      (347x288x578, mu jittered): A_h of 48 seeded reflections
+                      over all its stride-sampled voxels, and the per-leg
+                      detail of 1 reflection on 2,048 voxels.
 """
 from __future__ import annotations
 
@@ -43,6 +56,9 @@ sys.path.insert(0, ROOT)
 
 from anacor_public_gb300 import synth  # noqa: E402
 from oracle import oracle as orc  # noqa: E402
+
+# the reference checkout's C sources, compiled into oracle/_ref
+REFERENCE_SRC = os.environ.get("ANACOR_REFERENCE_SRC", "/root/reference/AnACor/src")
 
 # analytic sphere transmission factors at 2theta = linspace(0, 180, 10)
 # (AnACor/verification/sphere_verification_new.py:31-36)
@@ -179,9 +195,58 @@ def bisection_and_gridding(ref):
     print("ib", ib[4][:3], "grid", vals[0][:3])
 
 
+def _legs(ref, s, k, coords):
+    """Reference per-voxel, per-leg detail of reflection k of sample s."""
+    xr, sr = orc.Oracle().rotate(s, int(k))
+    d = ref.leg_detail(coords, sr, xr, s.voxel, s.label)
+    return {key: d[key] for key in ("face", "len", "nseg", "first", "last", "L")}
+
+
+def large_fixtures(ref):
+    nw = os.cpu_count() or 1
+    b = synth.beamline_sample()
+    rsel = np.arange(256, dtype=np.int64) * (b.n_refl // 256)
+    ah = ref.overall(b.subset(refl=rsel), num_workers=nw)
+    np.savez_compressed(os.path.join(HERE, "beamline_ah256.npz"), refl=rsel, ah=ah, digest=sample_digest(b))
+    print("beamline256", ah[:3])
+    del b
+
+    h = synth.high_absorption_sample()
+    rng = np.random.default_rng(44)
+    vsel = np.sort(rng.choice(len(h.coords), 32768, replace=False)).astype(np.int32)
+    rsel = np.sort(rng.choice(h.n_refl, 48, replace=False)).astype(np.int64)
+    hs = h.subset(refl=rsel, coords=h.coords[vsel])
+    ah = ref.overall(hs, num_workers=nw)
+    lsel = np.arange(0, len(vsel), 16)
+    legs = [_legs(ref, hs, k, hs.coords[lsel]) for k in (0, 1)]
+    np.savez_compressed(os.path.join(HERE, "highabs_ah.npz"), refl=rsel, voxels=vsel, ah=ah, digest=sample_digest(h),
+                        leg_refl=np.array([0, 1]), leg_voxels=lsel,
+                        **{f"leg_{key}": np.array([g[key] for g in legs]) for key in legs[0]})
+    print("highabs", ah[:3])
+    del h, hs
+
+    bs = synth.batch_samples()
+    k = int(np.argmax([np.prod(x.label.shape) for x in bs]))
+    s = bs[k]
+    del bs
+    rng = np.random.default_rng(45)
+    rsel = np.sort(rng.choice(s.n_refl, 48, replace=False)).astype(np.int64)
+    ss = s.subset(refl=rsel)
+    ah = ref.overall(ss, num_workers=nw)
+    lsel = np.linspace(0, len(s.coords), 2048, endpoint=False).astype(np.int64)
+    legs = [_legs(ref, ss, 0, s.coords[lsel])]
+    np.savez_compressed(os.path.join(HERE, "batch_ah.npz"), sample=k, refl=rsel, ah=ah, digest=sample_digest(s),
+                        leg_refl=np.array([0]), leg_voxels=lsel,
+                        **{f"leg_{key}": np.array([g[key] for g in legs]) for key in legs[0]})
+    print("batch", k, s.label.shape, len(s.coords), ah[:3])
+
+
 def main():
-    orc.build_oracle(ref=True)
+    orc.build_oracle(ref_src=REFERENCE_SRC)
     ref = orc.Reference()
+    if "--large" in sys.argv:
+        large_fixtures(ref)
+        return
     if "--modes" in sys.argv:
         bisection_and_gridding(ref)
         return

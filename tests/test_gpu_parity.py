@@ -196,6 +196,49 @@ def test_empty_inputs(lib, small):
     assert np.isnan(tracer.sample_absorption(e)).all()   # the reference's 0/0 mean
 
 
+@pytest.mark.parametrize("which", ["s1", "xray"])
+@pytest.mark.parametrize("bad", [np.nan, np.inf, 0.0])
+def test_non_finite_or_zero_direction_is_an_error(lib, small, which, bad):
+    """A NaN, infinite or zero-length s1 or incident beam: NULL from the drop-in
+    and ANACOR_ERR_DIRECTION (7), a raised error from the flat entry point, and
+    the next good call unaffected (host-side input, no kernel sees it)."""
+    s = small.subset(refl=slice(0, 6))
+    s1 = np.array(s.s1, copy=True)
+    xray = np.array(s.xray, copy=True)
+    if which == "s1":
+        s1[4] = bad
+    else:
+        xray[:] = bad
+    t = synth.Sample(label=s.label, coords=s.coords, s1=s1, omega=s.omega, xray=xray, omega_axis=s.omega_axis,
+                     F=s.F, voxel=s.voxel, mu=s.mu)
+    tab, keep = row_table(s.label)
+    res = lib.ray_tracing_overall(0, 6, t.coords, len(t.coords), t.s1, t.omega, t.xray, t.omega_axis, t.F, 6,
+                                  t.voxel, t.mu, tab, t.shape, 0, 0, 1, 1)
+    assert not res
+    assert lib.anacor_last_status() == 7
+    with pytest.raises(_lib.AnacorError) as ei:
+        tracer.sample_absorption(t)
+    assert ei.value.status == 7
+    good = lib.ray_tracing_overall(0, 6, s.coords, len(s.coords), s.s1, s.omega, s.xray, s.omega_axis, s.F, 6,
+                                   s.voxel, s.mu, tab, s.shape, 0, 0, 1, 1)
+    assert good
+    got = [good[i] for i in range(6)]
+    lib.free(ct.cast(good, ct.c_void_p))
+    assert max_rel(got, tracer.sample_absorption(s)) == 0.0
+
+
+def test_block_shape_guard(lib):
+    """The absorption kernel refuses a block shape its shared arrays are not
+    sized for: status bit 1 << ANACOR_ERR_ARGS, no access (128 threads: inside
+    the arrays, so even an unguarded kernel would stay in bounds)."""
+    word = ct.c_int32(-1)
+    assert lib.anacor_block_guard_check(128, ct.byref(word)) == 0, lib.anacor_last_error()
+    assert word.value == 1 << 3
+    assert lib.anacor_block_guard_check(256, ct.byref(word)) == 0
+    assert word.value == 0
+    assert lib.anacor_block_guard_check(300, ct.byref(word)) == 3   # refused on the host
+
+
 # --------------------------------------------------- the reference's ABI --
 
 def test_dropin_ray_tracing_overall_like_anacor_worker(lib, small, golden_dir):

@@ -43,6 +43,28 @@ def test_oracle_matches_reference_beamline_subset(oracle, golden_dir):
     assert np.array_equal(ah, g["ah"])
 
 
+def test_oracle_matches_reference_beamline_workload(oracle, golden_dir):
+    """32 of the 256 reference A_h of the 20,000-reflection beamline workload."""
+    g = np.load(os.path.join(golden_dir, "beamline_ah256.npz"))
+    b = synth.beamline_sample()
+    assert str(g["digest"]) == sample_digest(b)
+    k = np.arange(0, 256, 8)
+    ah = oracle.overall(b.subset(refl=g["refl"][k]), threads=os.cpu_count() or 1)
+    assert np.array_equal(ah, g["ah"][k])
+
+
+def test_oracle_matches_reference_largest_batch_sample(oracle, golden_dir):
+    g = np.load(os.path.join(golden_dir, "batch_ah.npz"))
+    s = synth.batch_samples(only=int(g["sample"]))[0]
+    assert str(g["digest"]) == sample_digest(s)
+    ss = s.subset(refl=g["refl"])
+    assert np.array_equal(oracle.overall(ss, threads=os.cpu_count() or 1), g["ah"])
+    xr, sr = oracle.rotate(ss, 0)
+    d = oracle.leg_detail(s.coords[g["leg_voxels"]], sr, xr, s.voxel, s.label)
+    for key in ("face", "len", "nseg", "L"):
+        assert np.array_equal(d[key], g[f"leg_{key}"][0]), key
+
+
 def test_oracle_sphere_known_answers(oracle, golden_dir):
     g = np.load(os.path.join(golden_dir, "sphere_kat.npz"))
     vol = sphere_volume(24)

@@ -1,8 +1,9 @@
 """anacor_absorption_noalloc: the absorption path for callers that cannot
-allocate device memory (e.g. code running while another component records a
-CUDA graph, or hosts whose device memory is owned by a pool they do not
-control).  Its scratch is a fixed file-scope device array, so it must give
-the same A_h as the allocating entry point, call after call, and reject
+allocate device memory (hosts whose device memory is owned by a pool they do
+not control, or pipelines that forbid allocation after start-up because
+cudaMalloc and cudaFree may synchronise the device).  Its scratch is a fixed
+file-scope device array, so it must give the same A_h as the allocating entry
+point, call after call, leave the device's free memory unchanged, and reject
 requests that do not fit that array.
 
 This file is collected last on purpose."""
@@ -64,3 +65,49 @@ def test_noalloc_rejects_requests_beyond_its_array():
                                      s.omega_axis, s.F, s.voxel, s.mu, 0, 1, ct.c_void_p(d_out.data_ptr()), None)
     assert st == 3
     assert "scratch" in _lib.last_error(L)[1]
+
+
+def test_noalloc_leaves_device_free_memory_unchanged():
+    import torch
+    build.build()
+    L = _lib.load()
+    base = synth.small_sample(n_refl=64, seed=5)
+    small = base.subset(refl=slice(0, 16), coords=base.coords[::3])
+    d_label = torch.from_numpy(base.label).cuda()
+    d_big = torch.from_numpy(np.ascontiguousarray(base.coords)).cuda()
+    d_small = torch.from_numpy(np.ascontiguousarray(small.coords)).cuda()
+    d_out = torch.zeros(base.n_refl, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    # warm-up call: loads the kernels' modules and does the per-device set-up
+    assert _call(L, small, d_label.data_ptr(), d_small.data_ptr(), d_out.data_ptr(), stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    # a larger request than the warm-up: more scratch used, no more memory taken
+    assert _call(L, base, d_label.data_ptr(), d_big.data_ptr(), d_out.data_ptr(), stream.cuda_stream) == 0, \
+        _lib.last_error(L)
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0
+
+
+def test_noalloc_reports_bad_directions_and_stays_usable():
+    import torch
+    build.build()
+    L = _lib.load()
+    s = synth.small_sample(n_refl=8, seed=7)
+    d_label = torch.from_numpy(s.label).cuda()
+    d_coords = torch.from_numpy(np.ascontiguousarray(s.coords)).cuda()
+    d_out = torch.zeros(s.n_refl, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    for bad in (np.nan, np.inf, 0.0):
+        t = s.subset(refl=slice(0, 8))
+        t.s1 = np.array(s.s1, copy=True)
+        t.s1[5] = bad
+        st = _call(L, t, d_label.data_ptr(), d_coords.data_ptr(), d_out.data_ptr(), stream.cuda_stream)
+        assert st == 7, (bad, _lib.last_error(L))   # ANACOR_ERR_DIRECTION
+    # the next good call is unaffected
+    want = tracer.sample_absorption(s)
+    assert _call(L, s, d_label.data_ptr(), d_coords.data_ptr(), d_out.data_ptr(), stream.cuda_stream) == 0
+    torch.cuda.synchronize()
+    got = d_out.cpu().numpy()
+    assert np.max(np.abs(got - want) / want) <= RTOL

@@ -73,10 +73,13 @@ std::mutex g_mu;
 DeviceState g_dev[64];
 
 // Plan-level variants: 1..4 cooperative march, 5..8 the centred distance
-// field, 9..12 the octant fields; 9..12 run the kernels of 5..8.
-constexpr int kPlanVariants = 12;
-int kernel_variant(int v) { return v > kVariants ? v - 4 : v; }
+// field, 9..12 the octant fields, 13..16 the octant fields in 4^3 bricks;
+// 9..12 run the kernels of 5..8 (linear fields), 13..16 those of 9..12.
+constexpr int kPlanVariants = 16;
+int kernel_variant(int v) { return v > 8 ? v - 4 : v; }
 int budget_of(int v) { return v > 0 ? (v - 1) % 4 + 1 : absorption_variant(); }
+// field a plan variant marches on: 0 none, 1 centred, 2 octant, 3 bricked octant
+int field_kind(int v) { return v <= 4 ? 0 : (v <= 8 ? 1 : (v <= 12 ? 2 : 3)); }
 
 // CTAs per SM of `variant` (0: the process default) on this device
 int variant_occupancy(DeviceState *d, int variant)
@@ -242,6 +245,8 @@ struct anacor_plan {
     int field_state = 0;           // 0 not built, 1 built, -1 labels outside 0..7 (no field)
     uint8_t *d_field8 = nullptr;   // the 8 octant fields, built on first use by variants 9..12
     int field8_state = 0;
+    uint8_t *d_field8b = nullptr;  // the same in 4^3 bricks, built on first use by variants 13..16
+    int field8b_state = 0;
 };
 
 namespace {
@@ -263,6 +268,7 @@ void plan_release(anacor_plan *p)
     dev_free(p->d_c64, st);
     dev_free(p->d_field, st);
     dev_free(p->d_field8, st);
+    dev_free(p->d_field8b, st);
     dev_free(p->d_order, st);
     if (p->h_refl && !p->h_refl_borrowed)
         cudaFreeHost(p->h_refl);
@@ -496,6 +502,29 @@ int plan_reserve_refl(anacor_plan *p, int64_t n_refl)
 // centred field (variants 5..8), kind 2 the 8 octant fields (9..12).
 int plan_ensure_field(anacor_plan *p, int kind = 1)
 {
+    if (kind == 3) {
+        // the bricked copy of the octant fields
+        if (p->field8b_state == 1)
+            return kOk;
+        if (p->field8b_state < 0)
+            return fail(kErrUnsupported, "bricked fields need fewer than 2^31 bytes per field");
+        const size_t per = brick_field_bytes(p->dims);
+        if (per >= (size_t)INT32_MAX) {
+            p->field8b_state = -1;
+            return fail(kErrUnsupported, "bricked fields need fewer than 2^31 bytes per field");
+        }
+        if (int st = plan_ensure_field(p, 2))
+            return st;
+        cudaError_t e;
+        if ((e = dev_alloc(&p->d_field8b, per * 8, p->stream)) ||
+            (e = launch_brick_fields(p->d_field8, p->dims, 8, p->d_field8b, p->stream)) ||
+            (e = cudaStreamSynchronize(p->stream))) {
+            dev_free(p->d_field8b, p->stream);
+            return cuda_fail(e, "bricked fields");
+        }
+        p->field8b_state = 1;
+        return kOk;
+    }
     uint8_t *&field = kind == 2 ? p->d_field8 : p->d_field;
     int &state = kind == 2 ? p->field8_state : p->field_state;
     if (state == 1)
@@ -534,10 +563,24 @@ int plan_ensure_field(anacor_plan *p, int kind = 1)
 // whether the plan's configured variant marches on a field it has
 bool plan_marches_field(const anacor_plan *p)
 {
-    return p->variant > kVariants ? p->field8_state == 1 : (p->variant > 4 && p->field_state == 1);
+    switch (field_kind(p->variant)) {
+    case 1: return p->field_state == 1;
+    case 2: return p->field8_state == 1;
+    case 3: return p->field8b_state == 1;
+    default: return false;
+    }
 }
 
-SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
+// whether that field is the bricked one
+bool plan_field_bricked(const anacor_plan *p)
+{
+    return field_kind(p->variant) == 3 && p->field8b_state == 1;
+}
+
+// The plan's sample as a launch descriptor; fk >= 0 names the field it
+// marches on (0 none, 1 centred, 2 octant, 3 bricked octant; the field must be
+// built), else the field of the plan's own variant.
+SampleDesc plan_desc(const anacor_plan *p, long long work_begin, int fk = -1)
 {
     SampleDesc d;
     std::memset(&d, 0, sizeof(d));
@@ -568,7 +611,16 @@ SampleDesc plan_desc(const anacor_plan *p, long long work_begin)
     d.qtab = p->d_qtab;
     d.work_begin = work_begin;
     d.order = p->n_refl > 0 ? p->d_order : nullptr;
-    if (p->variant > kVariants) {
+    if (fk < 0)
+        fk = field_kind(p->variant);
+    if (fk == 0) {
+        d.field = nullptr;
+        d.field_stride = 0;
+    } else if (fk == 3) {
+        d.field = p->field8b_state == 1 ? p->d_field8b : nullptr;
+        d.field_stride = (long long)brick_field_bytes(p->dims);
+        brick_strides(p->dims, &d.brick_sy, &d.brick_sz);
+    } else if (fk == 2) {
         d.field = p->field8_state == 1 ? p->d_field8 : nullptr;
         d.field_stride = (long long)p->dims[0] * p->dims[1] * p->dims[2];
     } else {
@@ -727,7 +779,7 @@ int plan_configure(anacor_plan *p, int variant, int tile, int order)
         order < -1 || order >= kVoxelOrders)
         return fail(kErrArgs, "bad plan configuration");
     if (variant > 4)
-        if (int st = plan_ensure_field(p, variant > kVariants ? 2 : 1))
+        if (int st = plan_ensure_field(p, field_kind(variant)))
             return st;
     cudaError_t e;
     if (order >= 0 && order != p->order && p->n_vox > 0) {
@@ -818,7 +870,7 @@ bool tune_lookup(const anacor_plan *p, TuneVal &v)
 int plan_default_config(anacor_plan *p)
 {
     TuneVal v{0, 0, 1, 0.0f};
-    if (tune_lookup(p, v) && (v.variant <= 4 || plan_ensure_field(p, v.variant > kVariants ? 2 : 1) == kOk))
+    if (tune_lookup(p, v) && (v.variant <= 4 || plan_ensure_field(p, field_kind(v.variant)) == kOk))
         return plan_configure(p, v.variant, v.tile, v.order);
     int variant = 0;
     const int big = std::max(p->dims[0], std::max(p->dims[1], p->dims[2]));
@@ -867,22 +919,38 @@ struct anacor_batch {
 
 namespace {
 
+// The batch's samples as descriptors.  Under a field variant every sample
+// marches on its field of that kind (built here if needed), so the batch is
+// one launch; a sample whose labels allow no field (outside 0..7) runs in a
+// first, cooperative launch of the same register budget.
 int batch_upload(anacor_batch *b)
 {
     std::vector<anacor_plan *> coop, field;
-    for (anacor_plan *p : b->plans)
-        (b->variant > 4 && plan_marches_field(p) ? field : coop).push_back(p);
+    const int fk = field_kind(b->variant);
+    for (anacor_plan *p : b->plans) {
+        if (fk > 0) {
+            const int st = plan_ensure_field(p, fk);
+            if (st == kOk) {
+                field.push_back(p);
+                continue;
+            }
+            if (st != kErrUnsupported)
+                return st;
+            succeed();   // no field for these labels: the cooperative group
+        }
+        coop.push_back(p);
+    }
     std::vector<SampleDesc> descs, descs_field;
     long long total = 0, items_coop = 0;
     for (anacor_plan *p : coop) {
-        descs.push_back(plan_desc(p, total));
+        descs.push_back(plan_desc(p, total, 0));
         total += (long long)p->n_refl * p->tiles;
     }
     items_coop = total;
     long long rebased = 0;
     for (anacor_plan *p : field) {
-        descs.push_back(plan_desc(p, total));
-        descs_field.push_back(plan_desc(p, rebased));
+        descs.push_back(plan_desc(p, total, fk));
+        descs_field.push_back(plan_desc(p, rebased, fk));
         const long long n = (long long)p->n_refl * p->tiles;
         total += n;
         rebased += n;
@@ -896,7 +964,7 @@ int batch_upload(anacor_batch *b)
     b->items_coop = items_coop;
     b->items_field = rebased;
     b->grid_coop = items_coop ? grid_for(dev, cv, items_coop) : 0;
-    b->grid_field = rebased ? grid_for(dev, cv + 4, rebased) : 0;
+    b->grid_field = rebased ? grid_for(dev, b->variant, rebased) : 0;
     cudaError_t e;
     if ((e = cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(SampleDesc) * descs.size(), cudaMemcpyHostToDevice,
                              b->stream)) ||
@@ -931,7 +999,7 @@ cudaError_t batch_enqueue(anacor_batch *b, cudaStream_t st)
         e = launch_absorption(b->d_descs, b->n_coop, b->items_coop, b->d_counter, b->grid_coop, st, cv);
     if (e == cudaSuccess && b->items_field > 0)
         e = launch_absorption(b->d_descs_field, b->n_field, b->items_field, b->d_counter_field, b->grid_field, st,
-                              cv + 4);
+                              kernel_variant(b->variant));
     return e;
 }
 
@@ -1296,8 +1364,8 @@ int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream)
         // one launch: the field march only when every sample marches on a field
         int variant = kernel_variant(p0->variant);
         for (int i = 0; i < n_plans && variant > 4; i++)
-            if (!plan_marches_field(plans[i]))
-                variant -= 4;
+            if (!plan_marches_field(plans[i]) || plan_field_bricked(plans[i]) != plan_field_bricked(p0))
+                variant = budget_of(p0->variant);
         const int grid = grid_for(p0->dev, variant, total);
         if ((e = launch_absorption(d_descs, n_plans, total, p0->d_counter, grid, st, variant)))
             return cuda_fail(e, "kernel launch");
@@ -1625,7 +1693,7 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
     TuneVal cv{0, 0, 1, 0.0f};
     const bool cached = tune_lookup(p, cv);
     // a cached distance-field choice does not apply to a volume without a field
-    if (cached && (cv.variant <= 4 || plan_ensure_field(p, cv.variant > kVariants ? 2 : 1) == kOk)) {
+    if (cached && (cv.variant <= 4 || plan_ensure_field(p, field_kind(cv.variant)) == kOk)) {
         if (best_ms)
             *best_ms = cv.ms;
         return plan_configure(p, cv.variant, cv.tile, cv.order) ? t_status : succeed();
@@ -1675,6 +1743,8 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
         variants.insert(variants.end(), {6, 7, 8});
     if (plan_ensure_field(p, 2) == kOk)
         variants.insert(variants.end(), {10, 11, 12});
+    if (plan_ensure_field(p, 3) == kOk)
+        variants.insert(variants.end(), {14, 15, 16});
     for (int tile : {128, 256, 512, 1024, 2048})
         for (int variant : variants) {
             float t = 0.0f;
@@ -1808,14 +1878,24 @@ int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl)
         if (p->n_refl > 0 && p->n_vox > 0)
             if (int st = anacor_plan_autotune(p, sample_refl, nullptr))
                 return st;
+    // then one variant for the whole launch: the cooperative march, or every
+    // sample on its centred, octant or bricked octant fields
     float best = 1e30f;
     int best_v = 0;
     std::vector<int> variants{2, 3, 4};
-    bool fields = false;
-    for (anacor_plan *p : b->plans)
-        fields = fields || plan_marches_field(p);
-    if (fields)
-        variants.insert(variants.end(), {6, 7, 8});
+    for (int fk = 1; fk <= 3; fk++) {
+        bool any = false;
+        for (anacor_plan *p : b->plans) {
+            const int st = plan_ensure_field(p, fk);
+            if (st && st != kErrUnsupported)
+                return st;
+            any = any || st == kOk;
+        }
+        succeed();
+        if (any)
+            for (int budget = 2; budget <= 4; budget++)
+                variants.push_back(4 * fk + budget);
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

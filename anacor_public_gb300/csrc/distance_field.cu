@@ -229,4 +229,67 @@ cudaError_t launch_octant_fields(const int8_t *d_vol, const int *dims, uint8_t *
     return cudaGetLastError();
 }
 
+namespace {
+
+// One thread per 16 output bytes (a 4x4 (y, x) slab of one brick row z).
+__global__ void brick_fields_kernel(const uint8_t *__restrict__ lin, int dz, int dy, int dx, int nbz, int nby,
+                                    int nbx, long long n_fields, uint8_t *__restrict__ out)
+{
+    const long long nvol = (long long)dz * dy * dx;
+    const long long per = (long long)nbz * nby * nbx * 64;
+    const long long total = n_fields * (per >> 4);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long f = q / (per >> 4);
+        const long long r = q - f * (per >> 4);       // 16-byte slab within the field
+        const long long brick = r >> 2;
+        const int zl = (int)(r & 3);
+        const int bx = (int)(brick % nbx);
+        const int by = (int)((brick / nbx) % nby);
+        const int bz = (int)(brick / ((long long)nbx * nby));
+        const int z = bz * 4 + zl;
+        uint32_t w[4];
+#pragma unroll
+        for (int yl = 0; yl < 4; yl++) {
+            const int y = by * 4 + yl;
+            uint32_t word = 0;
+#pragma unroll
+            for (int xl = 0; xl < 4; xl++) {
+                const int x = bx * 4 + xl;
+                const uint32_t b = (z < dz && y < dy && x < dx) ? lin[f * nvol + ((long long)z * dy + y) * dx + x] : 0u;
+                word |= b << (8 * xl);
+            }
+            w[yl] = word;
+        }
+        reinterpret_cast<uint4 *>(out + f * per)[r] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+}  // namespace
+
+size_t brick_field_bytes(const int *dims)
+{
+    return (size_t)((dims[0] + 3) / 4) * ((dims[1] + 3) / 4) * ((dims[2] + 3) / 4) * 64;
+}
+
+void brick_strides(const int *dims, int *sy, int *sz)
+{
+    const int nbx = (dims[2] + 3) / 4, nby = (dims[1] + 3) / 4;
+    *sy = 64 * nbx;
+    *sz = 64 * nbx * nby;
+}
+
+cudaError_t launch_brick_fields(const uint8_t *d_lin, const int *dims, int n_fields, uint8_t *d_out,
+                                cudaStream_t st)
+{
+    const int nbz = (dims[0] + 3) / 4, nby = (dims[1] + 3) / 4, nbx = (dims[2] + 3) / 4;
+    const long long total = (long long)n_fields * nbz * nby * nbx * 4;
+    if (total <= 0)
+        return cudaSuccess;
+    const int threads = 256;
+    const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 152ll * 64);
+    brick_fields_kernel<<<blocks, threads, 0, st>>>(d_lin, dims[0], dims[1], dims[2], nbz, nby, nbx, n_fields, d_out);
+    return cudaGetLastError();
+}
+
 }  // namespace anacor

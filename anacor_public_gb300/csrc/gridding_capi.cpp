@@ -612,7 +612,109 @@ int anacor_gridding_interpolate_async(anacor_gridding *g, const double *s1, cons
     return report_status(kOk, "");
 }
 
+}  // extern "C"
+
 // ---------------------------------------------------- reference drop-ins
+
+namespace {
+
+// The volume of the single-voxel drop-ins (ray_tracing_single_gridding,
+// ib_single_gridding), kept on the device between calls with the same row
+// table (address and shape); a caller that changes the volume's contents in
+// place between calls must pass a new table.
+struct SingleCache {
+    const int8_t *base = nullptr;
+    int64_t shape[3] = {0, 0, 0};
+    double voxel[3] = {0, 0, 0};
+    int full = -1;
+    anacor_plan *plan = nullptr;
+    short4 *d_coord = nullptr;
+    ReflTable *d_dir = nullptr;
+    double *d_val = nullptr;
+    double *d_vox_mu = nullptr;   // voxel[3], mu[4] (bisection)
+    MapDesc *d_desc = nullptr;
+    unsigned long long *d_counter = nullptr;
+    int *d_status = nullptr;
+    int dev = -1;
+};
+std::mutex g_single_mu;
+SingleCache g_single;
+
+// Argument checks of the single-voxel drop-ins, the cached volume, and the
+// voxel and direction uploaded on the plan's stream (caller holds
+// g_single_mu).  Status as report_status.
+int single_setup(int64_t *coord, const double *rotated_s1, double theta, double phi, double *voxel_size,
+                 double *coefficients, int8_t ***label_list, int64_t *shape, int full_iteration, int IsExp,
+                 PlanView &pv)
+{
+    if (!coord || !rotated_s1 || !voxel_size || !coefficients || !label_list || !shape)
+        return report_status(kErrArgs, "null argument");
+    // the reference asserts that the given angles are the vector's (to 1e-6)
+    double th, ph;
+    polar_angles(rotated_s1, false, &th, &ph);
+    if (!(std::fabs(th - theta) < 1e-6) || !(std::fabs(ph - phi) < 1e-6))
+        return report_status(kErrAssert, "theta/phi do not belong to rotated_s1 (the reference asserts here)");
+    for (int a = 0; a < 3; a++)
+        if (shape[a] <= 0 || shape[a] > kMaxDim || coord[a] < 0 || coord[a] >= shape[a])
+            return report_status(kErrArgs, "a coordinate lies outside the volume");
+    SingleCache &c = g_single;
+    const int8_t *base = label_list[0] ? label_list[0][0] : nullptr;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!base)
+        return report_status(kErrArgs, "empty label table");
+    if (c.plan && (c.base != base || std::memcmp(c.shape, shape, sizeof(c.shape)) ||
+                   std::memcmp(c.voxel, voxel_size, sizeof(c.voxel)) || c.full != full_iteration || c.dev != dev)) {
+        anacor_plan_destroy(c.plan);
+        c.plan = nullptr;
+    }
+    if (!c.plan) {
+        // the row table must be one C-contiguous block (utils_os.py:45-68)
+        const int64_t Y = shape[1], X = shape[2];
+        for (int64_t z = 0; z < shape[0]; z++)
+            for (int64_t y = 0; y < Y; y++)
+                if (!label_list[z] || label_list[z][y] != base + (z * Y + y) * X)
+                    return report_status(kErrArgs, "label table rows are not one contiguous volume");
+        const int64_t none[3] = {0, 0, 0};
+        c.plan = anacor_plan_create(base, shape, none, 0, voxel_size, coefficients, full_iteration, IsExp);
+        if (!c.plan)
+            return anacor_last_status();
+        if (!c.d_coord) {
+            cudaError_t e;
+            if ((e = dalloc(&c.d_coord, 1)) || (e = dalloc(&c.d_dir, 1)) || (e = dalloc(&c.d_val, 1)) ||
+                (e = dalloc(&c.d_vox_mu, 7)) || (e = dalloc(&c.d_desc, 1)) || (e = dalloc(&c.d_counter, 1)) ||
+                (e = dalloc(&c.d_status, 1)))
+                return cuda_err(e);
+        }
+        c.base = base;
+        std::memcpy(c.shape, shape, sizeof(c.shape));
+        std::memcpy(c.voxel, voxel_size, sizeof(c.voxel));
+        c.full = full_iteration;
+        c.dev = dev;
+    }
+    if (int st = plan_view(c.plan, &pv))
+        return st;
+    ReflTable tab;
+    if (setup_direction(rotated_s1, theta, phi, &tab))
+        return report_status(kErrDirection, "non-finite or zero direction vector");
+    const short4 cv = make_short4((short)coord[0], (short)coord[1], (short)coord[2], 0);
+    double vm[7];
+    for (int a = 0; a < 3; a++)
+        vm[a] = voxel_size[a];
+    for (int a = 0; a < 4; a++)
+        vm[3 + a] = coefficients[a];
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(c.d_coord, &cv, sizeof(cv), cudaMemcpyHostToDevice, pv.stream)) ||
+        (e = cudaMemcpyAsync(c.d_dir, &tab, sizeof(tab), cudaMemcpyHostToDevice, pv.stream)) ||
+        (e = cudaMemcpyAsync(c.d_vox_mu, vm, sizeof(vm), cudaMemcpyHostToDevice, pv.stream)) ||
+        (e = cudaStreamSynchronize(pv.stream)))
+        return cuda_err(e);
+    return kOk;
+}
+
+}  // namespace
+
+extern "C" {
 
 // ray_tracing_single_gridding (AnACor/src/ray_tracing.c:484-534): the map
 // value of one voxel for one direction.  The volume is kept on the device
@@ -624,99 +726,19 @@ double ray_tracing_single_gridding(int64_t *coord, const double *rotated_s1, dou
 {
     (void)index;
     const double nan = std::nan("");
-    if (!coord || !rotated_s1 || !voxel_size || !coefficients || !label_list || !shape) {
-        report_status(kErrArgs, "null argument");
-        return nan;
-    }
-    // the reference asserts that the given angles are the vector's (to 1e-6)
-    double th, ph;
-    polar_angles(rotated_s1, false, &th, &ph);
-    if (!(std::fabs(th - theta) < 1e-6) || !(std::fabs(ph - phi) < 1e-6)) {
-        report_status(kErrAssert, "theta/phi do not belong to rotated_s1 (the reference asserts here)");
-        return nan;
-    }
-    for (int a = 0; a < 3; a++)
-        if (shape[a] <= 0 || shape[a] > kMaxDim || coord[a] < 0 || coord[a] >= shape[a]) {
-            report_status(kErrArgs, "a coordinate lies outside the volume");
-            return nan;
-        }
-    static std::mutex mu;
-    static struct Cache {
-        const int8_t *base = nullptr;
-        int64_t shape[3] = {0, 0, 0};
-        double voxel[3] = {0, 0, 0};
-        int full = -1;
-        anacor_plan *plan = nullptr;
-        short4 *d_coord = nullptr;
-        ReflTable *d_dir = nullptr;
-        double *d_val = nullptr;
-        MapDesc *d_desc = nullptr;
-        unsigned long long *d_counter = nullptr;
-        int *d_status = nullptr;
-        int dev = -1;
-    } c;
-    std::lock_guard<std::mutex> lk(mu);
-    const int8_t *base = label_list[0] ? label_list[0][0] : nullptr;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (!base) {
-        report_status(kErrArgs, "empty label table");
-        return nan;
-    }
-    if (c.plan && (c.base != base || std::memcmp(c.shape, shape, sizeof(c.shape)) ||
-                   std::memcmp(c.voxel, voxel_size, sizeof(c.voxel)) || c.full != full_iteration || c.dev != dev)) {
-        anacor_plan_destroy(c.plan);
-        c.plan = nullptr;
-    }
-    if (!c.plan) {
-        // the row table must be one C-contiguous block (utils_os.py:45-68)
-        const int64_t Y = shape[1], X = shape[2];
-        for (int64_t z = 0; z < shape[0]; z++)
-            for (int64_t y = 0; y < Y; y++)
-                if (!label_list[z] || label_list[z][y] != base + (z * Y + y) * X) {
-                    report_status(kErrArgs, "label table rows are not one contiguous volume");
-                    return nan;
-                }
-        const int64_t none[3] = {0, 0, 0};
-        c.plan = anacor_plan_create(base, shape, none, 0, voxel_size, coefficients, full_iteration, IsExp);
-        if (!c.plan)
-            return nan;
-        if (!c.d_coord) {
-            cudaError_t e;
-            if ((e = dalloc(&c.d_coord, 1)) || (e = dalloc(&c.d_dir, 1)) || (e = dalloc(&c.d_val, 1)) ||
-                (e = dalloc(&c.d_desc, 1)) || (e = dalloc(&c.d_counter, 1)) || (e = dalloc(&c.d_status, 1))) {
-                cuda_err(e);
-                return nan;
-            }
-        }
-        c.base = base;
-        std::memcpy(c.shape, shape, sizeof(c.shape));
-        std::memcpy(c.voxel, voxel_size, sizeof(c.voxel));
-        c.full = full_iteration;
-        c.dev = dev;
-    }
+    std::lock_guard<std::mutex> lk(g_single_mu);
     PlanView pv;
-    if (plan_view(c.plan, &pv))
+    if (single_setup(coord, rotated_s1, theta, phi, voxel_size, coefficients, label_list, shape, full_iteration,
+                     IsExp, pv))
         return nan;
-    ReflTable tab;
-    if (setup_direction(rotated_s1, theta, phi, &tab)) {
-        report_status(kErrDirection, "non-finite or zero direction vector");
-        return nan;
-    }
-    const short4 cv = make_short4((short)coord[0], (short)coord[1], (short)coord[2], 0);
-    cudaStream_t st = pv.stream;
-    cudaError_t e;
-    if ((e = cudaMemcpyAsync(c.d_coord, &cv, sizeof(cv), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(c.d_dir, &tab, sizeof(tab), cudaMemcpyHostToDevice, st))) {
-        cuda_err(e);
-        return nan;
-    }
+    SingleCache &c = g_single;
     pv.coords = c.d_coord;
     pv.n_vox = 1;
     if (run_map(pv, c.d_dir, 1, IsExp ? 1 : 0, coefficients, nullptr, c.d_val, 1, nullptr, c.d_desc, c.d_counter,
-                c.d_status, 1, st))
+                c.d_status, 1, pv.stream))
         return nan;
     double v = 0.0;
+    cudaError_t e;
     if ((e = cudaMemcpy(&v, c.d_val, sizeof(double), cudaMemcpyDeviceToHost))) {
         cuda_err(e);
         return nan;
@@ -725,16 +747,43 @@ double ray_tracing_single_gridding(int64_t *coord, const double *rotated_s1, dou
     return v;
 }
 
-// ib_single_gridding (AnACor/src/ray_tracing.c:427-482): the bisection
-// variant is not implemented.
+// ib_single_gridding (AnACor/src/ray_tracing.c:427-482): the same value with
+// the diffracted leg's lengths found by iterative bisection (resolution 1.0,
+// num_cls 4 also searches bubble boundaries) instead of the march.  The
+// exponent sum_m mu_m (0 + L_m) comes from the GPU in cal_rate's order and
+// exp(-a) is taken here, with the host's libm as the reference takes it.
 double ib_single_gridding(int64_t *coord, const double *rotated_s1, double theta, double phi, double *voxel_size,
                           double *coefficients, int8_t ***label_list, int64_t *shape, int full_iteration, int index,
                           int num_cls, int IsExp)
 {
-    (void)coord; (void)rotated_s1; (void)theta; (void)phi; (void)voxel_size; (void)coefficients;
-    (void)label_list; (void)shape; (void)full_iteration; (void)index; (void)num_cls; (void)IsExp;
-    report_status(kErrUnsupported, "the bisection method is not implemented");
-    return std::nan("");
+    (void)index;
+    const double nan = std::nan("");
+    std::lock_guard<std::mutex> lk(g_single_mu);
+    PlanView pv;
+    if (single_setup(coord, rotated_s1, theta, phi, voxel_size, coefficients, label_list, shape, full_iteration,
+                     IsExp, pv))
+        return nan;
+    SingleCache &c = g_single;
+    cudaError_t e;
+    double a = 0.0;
+    int status = 0;
+    if ((e = launch_ib_direction(c.d_dir, pv.vol, pv.dims, c.d_coord, 1, c.d_vox_mu, num_cls, c.d_val, c.d_status,
+                                 pv.stream)) ||
+        (e = cudaMemcpyAsync(&a, c.d_val, sizeof(double), cudaMemcpyDeviceToHost, pv.stream)) ||
+        (e = cudaMemcpyAsync(&status, c.d_status, sizeof(int), cudaMemcpyDeviceToHost, pv.stream)) ||
+        (e = cudaStreamSynchronize(pv.stream))) {
+        cuda_err(e);
+        return nan;
+    }
+    if (status) {
+        report_status(status, status == kErrArgs ? "a bisection point left the volume (undefined in the reference)"
+                              : status == kErrAssert ? "exit face inconsistent with the ray angles (the reference "
+                                                       "asserts here)"
+                                                     : "the ray found no exit plane");
+        return nan;
+    }
+    report_status(kOk, "");
+    return IsExp ? std::exp(-a) : a;
 }
 
 // nearest_neighbor_interpolate_overall (AnACor/src/gridding_interpolation.c:

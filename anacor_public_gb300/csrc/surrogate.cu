@@ -609,6 +609,336 @@ __global__ void audit_kernel(const float *__restrict__ spread, long long n, uint
     flags[i] = (uint8_t)((h < cut ? 1u : 0u) | (!(sp <= threshold) ? 2u : 0u));
 }
 
+// ------------------------------------------------- fused inference kernel
+//
+// The four hidden layers and the head of every member for a 128-row tile in
+// one persistent kernel: the tile's Fourier features and each layer's
+// activations stay in shared memory, the accumulator in tensor memory, and
+// only the weights stream in (from L2: 1.7 MB for four members), as 32 KiB
+// K-chunks copied by the bulk-copy engine (cp.async.bulk) into a 3-stage ring.
+// One thread issues the tcgen05 MMAs; all eight warps run the epilogue (bias,
+// GELU, BF16 into the next layer's operand tile, or the head's dot product).
+// The arithmetic is the layered path's: same MMA sequence, the same epilogue
+// expressions and the head's and ensemble's summation orders, so the outputs
+// are the same numbers without the per-layer round trips through HBM.
+
+constexpr int kChunkBytes = kWidth * umma::kBK * 2;                    // one 256 x 64 BF16 weight chunk
+constexpr int kChunksPerMember = 1 + (kDepth - 1) * (kWidth / umma::kBK);  // 13
+constexpr int kInferStages = 3;
+constexpr int kInferThreads = 256;
+constexpr int kTileRows = umma::kBM;                                    // 128
+constexpr int kActChunk = kTileRows * umma::kBK * 2;                   // 16 KiB
+constexpr int kMemberConsts = kDepth * kWidth + kWidth + 2;             // biases, w5, b5, pad
+constexpr int kGStride = 33;                                            // head partials per row (32 + pad)
+constexpr int kOffInferAct = kInferStages * kChunkBytes;
+constexpr int kOffInferX0 = kOffInferAct + (kWidth / umma::kBK) * kActChunk;
+constexpr int kOffInferC = kOffInferX0 + kActChunk;
+constexpr int kOffInferG = kOffInferC + ((kMemberConsts * 4 + 15) / 16) * 16;
+constexpr int kOffInferY = kOffInferG + kTileRows * kGStride * 4;
+constexpr int kInferSmem = kOffInferY + kMaxMembers * kTileRows * 4;
+static_assert(kInferSmem <= 227 * 1024, "fused inference shared memory");
+
+struct WeightPtrs {
+    const bf16 *w[kDepth];
+};
+
+// The weight image: for every member its 13 K-chunks (layer 0: one, layers
+// 1..3: four each) of W_l [256][K], each in the canonical no-swizzle K-major
+// layout of a 256 x 64 tile, in the order the fused kernel consumes them.
+__global__ void weight_image_kernel(WeightPtrs W, int E, uint8_t *__restrict__ img)
+{
+    constexpr int kPieces = kChunkBytes / 16;   // 16-byte pieces (8 BF16 along K) per chunk
+    const long long total = (long long)E * kChunksPerMember * kPieces;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long c = t / kPieces;
+        const int p = (int)(t - c * kPieces);
+        const int e = (int)(c / kChunksPerMember);
+        const int q = (int)(c - (long long)e * kChunksPerMember);
+        const int l = q == 0 ? 0 : 1 + (q - 1) / (kWidth / umma::kBK);
+        const int kq = q == 0 ? 0 : (q - 1) % (kWidth / umma::kBK);
+        const int K = in_dim(l);
+        const int r = p >> 3, kc = p & 7;
+        const bf16 *src = W.w[l] + (long long)e * kWidth * K + (long long)r * K + kq * umma::kBK + kc * 8;
+        *reinterpret_cast<uint4 *>(img + c * kChunkBytes + umma::tile_off(r, kc * 8)) =
+            *reinterpret_cast<const uint4 *>(src);
+    }
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(umma::smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from global to this CTA's shared memory, completing on `bar`
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     umma::smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(umma::smem_u32(bar))
+                 : "memory");
+}
+
+struct InferArgs {
+    const float *x7;
+    long long n;
+    const float *Bf;
+    const uint8_t *wimg;
+    const float *params;
+    int E;
+    float mu, sd;
+    float *mean, *spread, *members;
+    long long ldm;
+    int *err;
+};
+
+// member constant i (biases of the four layers, w5, b5) from the FP32 masters
+__device__ __forceinline__ float member_const(const float *P, int i)
+{
+    if (i < kDepth * kWidth)
+        return P[off_b(i / kWidth) + (i % kWidth)];
+    if (i < kDepth * kWidth + kWidth)
+        return P[kOffW5 + (i - kDepth * kWidth)];
+    return i == kDepth * kWidth + kWidth ? P[kOffB5] : 0.0f;
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t full[kInferStages], empty[kInferStages], accb;
+    __shared__ uint32_t tslot;
+    uint8_t *Ws = smem;
+    uint8_t *Act = smem + kOffInferAct;
+    uint8_t *X0s = smem + kOffInferX0;
+    float *cst = reinterpret_cast<float *>(smem + kOffInferC);
+    float *gs = reinterpret_cast<float *>(smem + kOffInferG);
+    float *ys = reinterpret_cast<float *>(smem + kOffInferY);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long tiles = (a.n + kTileRows - 1) / kTileRows;
+    const long long my_tiles = tiles > (long long)blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const long long per_tile = (long long)a.E * kChunksPerMember;
+    const long long total = my_tiles * per_tile;
+
+    if (tid == 0) {
+        for (int s = 0; s < kInferStages; s++) {
+            umma::mbar_init(&full[s], 1);
+            umma::mbar_init(&empty[s], 1);
+        }
+        umma::mbar_init(&accb, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0)
+        umma::tmem_alloc(&tslot, kWidth);
+    umma::tc_fence_before();
+    __syncthreads();
+    umma::tc_fence_after();
+    const uint32_t tmem = tslot;
+    constexpr uint32_t idesc = umma::idesc_bf16_f32(kWidth);
+
+    bool ok = true;
+    long long q_issue = 0, q_use = 0;   // thread 0: next weight chunk to load / to consume
+    uint32_t acc_phase = 0;
+    // thread 0: load weight chunk q into stage q % kInferStages once the MMAs
+    // that read that stage's previous chunk are done
+    auto issue = [&](long long q) -> bool {
+        const int s = (int)(q % kInferStages);
+        if (q >= kInferStages && !umma::mbar_wait(&empty[s], (uint32_t)((q / kInferStages - 1) & 1)))
+            return false;
+        mbar_expect_tx(&full[s], kChunkBytes);
+        bulk_g2s(Ws + s * kChunkBytes, a.wimg + (q % per_tile) * kChunkBytes, kChunkBytes, &full[s]);
+        return true;
+    };
+    if (tid == 0)
+        for (; q_issue < total && q_issue < kInferStages - 1; q_issue++)
+            ok = issue(q_issue) && ok;
+
+    const int rl = 32 * (warp & 3) + lane;     // this thread's row of the tile (TMEM lane)
+    const int cb = (warp >> 2) * (kWidth / 2);  // first of its 128 accumulator columns
+    for (long long ti = 0; ti < my_tiles && ok; ti++) {
+        const long long row0 = (blockIdx.x + ti * gridDim.x) * kTileRows;
+        // Fourier features of the tile (features_kernel's expressions), BF16
+        // into the layer-0 operand tile; rows past n are zeros
+        {
+            const int r = tid >> 1, h = tid & 1;
+            const long long i = row0 + r;
+            float sv[16], cv[16];
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                sv[jj] = 0.0f;
+                cv[jj] = 0.0f;
+            }
+            if (i < a.n) {
+                const float *x = a.x7 + 7 * i;
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++) {
+                    const int j = 16 * h + jj;
+                    float p = 0.0f;
+#pragma unroll
+                    for (int q = 0; q < kIn; q++)
+                        p += a.Bf[j * kIn + q] * x[q];
+                    sincospif(2.0f * p, &sv[jj], &cv[jj]);
+                }
+            }
+#pragma unroll
+            for (int part = 0; part < 4; part++) {   // features 16h..16h+15 (sin) and 32+16h.. (cos)
+                const float *src = part < 2 ? sv + 8 * part : cv + 8 * (part - 2);
+                const int f0 = (part < 2 ? 0 : kFeat / 2) + 16 * h + 8 * (part & 1);
+                __align__(16) bf16 t[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++)
+                    t[q] = __float2bfloat16_rn(src[q]);
+                *reinterpret_cast<uint4 *>(X0s + umma::tile_off(r, f0)) = *reinterpret_cast<const uint4 *>(t);
+            }
+        }
+        umma::fence_async_smem();
+        for (int e = 0; e < a.E && ok; e++) {
+            __syncthreads();   // the previous member's head is done with cst
+            for (int i = tid; i < kMemberConsts; i += kInferThreads)
+                cst[i] = member_const(a.params + (long long)e * kParams, i);
+            for (int l = 0; l < kDepth; l++) {
+                const int nk = in_dim(l) / umma::kBK;
+                // the operand tile and the constants are written; the previous
+                // layer's accumulator reads are done
+                umma::tc_fence_before();
+                ok = __syncthreads_and(ok);
+                if (!ok)
+                    break;
+                if (tid == 0) {
+                    umma::tc_fence_after();
+                    for (int kc = 0; kc < nk && ok; kc++, q_use++) {
+                        const int s = (int)(q_use % kInferStages);
+                        if (!umma::mbar_wait(&full[s], (uint32_t)((q_use / kInferStages) & 1))) {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t a0 = umma::smem_u32(l == 0 ? X0s : Act + kc * kActChunk);
+                        const uint32_t b0 = umma::smem_u32(Ws + s * kChunkBytes);
+#pragma unroll
+                        for (int kk = 0; kk < umma::kBK / 16; kk++)
+                            umma::mma_bf16(tmem, umma::smem_desc(a0 + kk * 256, 128, 1024),
+                                           umma::smem_desc(b0 + kk * 256, 128, 1024), idesc,
+                                           (kc > 0 || kk > 0) ? 1u : 0u);
+                        umma::mma_commit(&empty[s]);
+                        if (q_issue < total) {
+                            ok = issue(q_issue) && ok;
+                            q_issue++;
+                        }
+                    }
+                    umma::mma_commit(&accb);
+                }
+                // the layer's accumulator (a failed issue leaves it
+                // uncommitted: the bounded wait then fails too)
+                ok = umma::mbar_wait(&accb, acc_phase) && ok;
+                acc_phase ^= 1u;
+                umma::tc_fence_after();
+                const float *bias = cst + l * kWidth;
+                const float *w5 = cst + kDepth * kWidth;
+                for (int c0 = cb; c0 < cb + kWidth / 2; c0 += 16) {
+                    float v[16];
+                    umma::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c0, v);
+#pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        v[q] = gelu(v[q] + bias[c0 + q]);
+                    __align__(16) bf16 t[16];
+#pragma unroll
+                    for (int q = 0; q < 16; q++)
+                        t[q] = __float2bfloat16_rn(v[q]);
+                    if (l < kDepth - 1) {
+                        uint8_t *dst = Act + (c0 / umma::kBK) * kActChunk;
+                        const int k = c0 % umma::kBK;
+                        *reinterpret_cast<uint4 *>(dst + umma::tile_off(rl, k)) = *reinterpret_cast<const uint4 *>(t);
+                        *reinterpret_cast<uint4 *>(dst + umma::tile_off(rl, k + 8)) =
+                            *reinterpret_cast<const uint4 *>(t + 8);
+                    } else {
+                        // the head's per-8-column partial sums, as head_kernel's lanes form them
+#pragma unroll
+                        for (int g = 0; g < 2; g++) {
+                            float acc = 0.0f;
+#pragma unroll
+                            for (int q = 0; q < 8; q++)
+                                acc += __bfloat162float(t[8 * g + q]) * w5[c0 + 8 * g + q];
+                            gs[rl * kGStride + (c0 + 8 * g) / 8] = acc;
+                        }
+                    }
+                }
+                umma::fence_async_smem();
+            }
+            ok = __syncthreads_and(ok);   // uniform again: every thread takes the same branch
+            if (!ok)
+                break;
+            if (tid < kTileRows) {
+                // head_kernel's shuffle tree over the 32 partial sums (lane 0's order)
+                float g[32];
+#pragma unroll
+                for (int j = 0; j < 32; j++)
+                    g[j] = gs[tid * kGStride + j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                    for (int j = 0; j < o; j++)
+                        g[j] = g[j] + g[j + o];
+                ys[e * kTileRows + tid] = g[0] + cst[kDepth * kWidth + kWidth];
+            }
+        }
+        ok = __syncthreads_and(ok);
+        if (!ok)
+            break;
+        if (tid < kTileRows && row0 + tid < a.n) {
+            // ensemble_kernel's statistics
+            const long long i = row0 + tid;
+            float av[kMaxMembers];
+            float sum = 0.0f;
+#pragma unroll
+            for (int e = 0; e < kMaxMembers; e++) {
+                if (e < a.E) {
+                    const float la = a.mu + a.sd * ys[e * kTileRows + tid];
+                    if (a.members)
+                        a.members[e * a.ldm + i] = la;
+                    av[e] = expf(la);
+                    sum += av[e];
+                }
+            }
+            const float m = sum / a.E;
+            float var = 0.0f;
+#pragma unroll
+            for (int e = 0; e < kMaxMembers; e++)
+                if (e < a.E)
+                    var += (av[e] - m) * (av[e] - m);
+            a.mean[i] = m;
+            a.spread[i] = sqrtf(var / a.E) / m;
+        }
+    }
+    if (tid == 0) {
+        // weight chunks still in flight complete before the CTA's shared
+        // memory goes away (bounded: a failed copy does not hold the exit)
+        for (long long q = q_use; q < q_issue; q++)
+            umma::mbar_wait(&full[q % kInferStages], (uint32_t)((q / kInferStages) & 1));
+        if (!ok)
+            atomicOr(a.err, 1);
+    }
+    umma::tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        umma::tmem_dealloc(tmem, kWidth);
+}
+
+std::once_flag g_infer_once[64];
+cudaError_t g_infer_init_err[64];
+
+// opt the fused kernel into its shared-memory size once per device
+cudaError_t infer_init(int dev)
+{
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    std::call_once(g_infer_once[dev], [dev] {
+        g_infer_init_err[dev] =
+            cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
+    });
+    return g_infer_init_err[dev];
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ state
@@ -641,6 +971,8 @@ struct anacor_surrogate {
     cudaGraphExec_t exec = nullptr;
     int graph_rows = 0;
     AdamArgs adam{1e-3f, 1e-5f, 0.9f, 0.999f, 1e-8f, 0u};
+    int fused = 1;                  // inference by the fused kernel (1) or layer by layer (0)
+    uint8_t *wimg = nullptr;        // the fused kernel's weight image
 };
 
 namespace {
@@ -958,7 +1290,7 @@ void anacor_surrogate_destroy(anacor_surrogate *s)
         cudaStreamSynchronize(s->st);
     free_work(s);
     dfree(s->params); dfree(s->m); dfree(s->v); dfree(s->grad); dfree(s->Bf);
-    dfree(s->loss_acc); dfree(s->step); dfree(s->err); dfree(s->loss_hist);
+    dfree(s->loss_acc); dfree(s->step); dfree(s->err); dfree(s->loss_hist); dfree(s->wimg);
     dfree(s->target); dfree(s->feat);
     for (int l = 0; l < kDepth; l++) {
         dfree(s->W[l]);
@@ -1201,6 +1533,40 @@ int anacor_surrogate_predict_device(anacor_surrogate *s, const float *d_x7, int6
     if (n == 0)
         return report_status(kOk, "");
     cudaStream_t st = stream ? (cudaStream_t)stream : s->st;
+    if (s->fused) {
+        // one launch over all n rows: no activation workspace
+        int dev = 0, sms = 0;
+        cudaError_t e;
+        if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) ||
+            (e = infer_init(dev)))
+            return cuda_fail(e);
+        if (!s->wimg && (e = dalloc(&s->wimg, (size_t)s->E * kChunksPerMember * kChunkBytes)))
+            return cuda_fail(e);
+        WeightPtrs wp;
+        for (int l = 0; l < kDepth; l++)
+            wp.w[l] = s->W[l];
+        weight_image_kernel<<<2 * sms, 256, 0, st>>>(wp, s->E, s->wimg);
+        InferArgs ia;
+        ia.x7 = d_x7;
+        ia.n = n;
+        ia.Bf = s->Bf;
+        ia.wimg = s->wimg;
+        ia.params = s->params;
+        ia.E = s->E;
+        ia.mu = (float)s->t_mean;
+        ia.sd = (float)s->t_std;
+        ia.mean = d_mean;
+        ia.spread = d_spread;
+        ia.members = d_members;
+        ia.ldm = n;
+        ia.err = s->err;
+        const long long tiles = (n + kTileRows - 1) / kTileRows;
+        const int grid = (int)std::min<long long>(tiles, sms);
+        infer_kernel<<<grid, kInferThreads, kInferSmem, st>>>(ia);
+        if ((e = cudaGetLastError()))
+            return cuda_fail(e);
+        return report_status(kOk, "");
+    }
     const int chunk = (int)std::min<int64_t>(kPredictChunk, (n + umma::kBM - 1) / umma::kBM * umma::kBM);
     if (s->rows != chunk || s->train_ws) {
         // the workspace is about to be replaced: nothing may still use it
@@ -1217,6 +1583,16 @@ int anacor_surrogate_predict_device(anacor_surrogate *s, const float *d_x7, int6
                                          d_members ? d_members + i0 : nullptr, n, st))
             return cuda_fail(e);
     }
+    return report_status(kOk, "");
+}
+
+int anacor_surrogate_set_inference(anacor_surrogate *s, int fused)
+{
+    if (!s || (fused != 0 && fused != 1))
+        return report_status(kErrArgs, "bad arguments");
+    if (s->st)
+        cudaStreamSynchronize(s->st);
+    s->fused = fused;
     return report_status(kOk, "");
 }
 

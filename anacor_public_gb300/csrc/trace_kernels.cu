@@ -85,7 +85,29 @@ struct Vol {
     int dz, dy, dx;
     const uint8_t *field = nullptr;   // label | distance << 3, for the distance-field march
     long long field_stride = 0;       // 0: one centred field; else 8 octant fields this far apart
+    int bsy = 0, bsz = 0;             // bricked fields: byte strides of a brick step in y and z
 };
+
+// Offset of voxel (z, y, x) in a field stored in 4x4x4 bricks of 64 bytes:
+// bricks in (z, y, x) order, bytes inside a brick (z, y, x) with x fastest, so
+// a 32-byte sector holds a 2x4x4 (z, y, x) box.  A ray that steps by one voxel
+// along any axis mostly stays in the sector its previous load brought into L1
+// (in the linear layout only steps along x do).
+__device__ __forceinline__ int brick_term(int u, int bs, int sh)
+{
+    return (u >> 2) * bs + ((u & 3) << sh);
+}
+
+__device__ __forceinline__ int brick_offset(int z, int y, int x, int bsy, int bsz)
+{
+    return brick_term(z, bsz, 4) + brick_term(y, bsy, 2) + brick_term(x, 64, 0);
+}
+
+// brick stride and in-brick shift of axis k (0 z, 1 y, 2 x)
+__device__ __forceinline__ int brick_stride(int k, const Vol &v)
+{
+    return k == 0 ? v.bsz : (k == 1 ? v.bsy : 64);
+}
 
 __device__ __forceinline__ int pick3(int k, int z, int y, int x)
 {
@@ -340,7 +362,7 @@ __device__ __noinline__ void march_lane(const FaceRule &R, int cz, int cy, int c
 // increment `inc`, from the reference's FP64 expression (an increment whose
 // fixed-point fraction lies near a rounding boundary).
 __device__ __noinline__ uint32_t exact_byte(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol v,
-                                            const uint8_t *bytes)
+                                            const uint8_t *bytes, bool brick)
 {
     int pz, py, px;
     const int s = G.count_axis;
@@ -348,12 +370,12 @@ __device__ __noinline__ uint32_t exact_byte(const FaceRule &G, int cz, int cy, i
     pz = s == 0 ? cz + inc * ds : exact_axis(cz, inc, G.q[0], G.use_round, v.dz);
     py = s == 1 ? cy + inc * ds : exact_axis(cy, inc, G.q[1], G.use_round, v.dy);
     px = s == 2 ? cx + inc * ds : exact_axis(cx, inc, G.q[2], G.use_round, v.dx);
-    return (uint32_t)__ldg(bytes + (pz * v.dy + py) * v.dx + px);
+    return (uint32_t)__ldg(bytes + (brick ? brick_offset(pz, py, px, v.bsy, v.bsz) : (pz * v.dy + py) * v.dx + px));
 }
 
 __device__ __forceinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol &v)
 {
-    return exact_byte(G, cz, cy, cx, inc, v, reinterpret_cast<const uint8_t *>(v.p));
+    return exact_byte(G, cz, cy, cx, inc, v, reinterpret_cast<const uint8_t *>(v.p), false);
 }
 
 // Increments i >= 0 for which c + i*q stays at least 2 voxels inside [0, h]
@@ -385,14 +407,20 @@ __device__ __forceinline__ int wall_increments(double q, int c, int h)
 // carries increment i's label: it is accepted without a load, and the march
 // goes on at i + nmax + 1.  Labels, stops, class changes and len_path_2 are
 // therefore exactly those of the per-increment march.
-// One lane's field march over one leg, as a chain of dependent loads.
+// One lane's field march over one leg, as a chain of dependent loads.  With
+// a bricked field (kBrick) the chain holds absolute coordinates instead of
+// linear strides (the members of the other layout are never set).
 struct FieldChain {
     const FaceRule *R;
     const uint8_t *fld;       // the field this leg marches on (its octant's)
-    const uint8_t *pk;        // fld + the leg's start voxel
-    long long off, Qa, Qb;
+    const uint8_t *pk;        // linear: fld + the leg's start voxel
+    long long off, Qa, Qb;    // bricked: off of axis a, offb of axis b, with the start coordinates
+    long long offb;
     uint32_t Ma, Mb, rq;
-    int dS, Sa, Sb;           // strides of the step axis (signed) and the two others
+    int dS, Sa, Sb;           // linear: strides of the step axis (signed) and the two others
+    int cs, ds;               // bricked: start coordinate and direction on the step axis
+    int bs_s, bs_a, bs_b;     // bricked: brick strides of the step axis and the two others
+    int sh_s, sh_a, sh_b;     // bricked: their in-brick shifts
     int i, lim, last, prev, nseg;
     bool on;
 };
@@ -402,21 +430,37 @@ __device__ __forceinline__ int field_nmax(uint32_t d, uint32_t rq)
     return d < 2u ? 0 : min((int)d - 1, (int)(((d - 2u) * rq) >> 16));
 }
 
+template <bool kBrick>
 __device__ __forceinline__ void chain_init(FieldChain &c, const FaceRule &R, const LegGeom &g, const uint8_t *fld,
-                                           int base, int lim, uint32_t b0, const March &m)
+                                           int base, int lim, uint32_t b0, const March &m, const Vol &v)
 {
     c.R = &R;
     c.fld = fld;
-    c.pk = fld + base;
-    c.off = g.off;
     c.Qa = g.Qa;
     c.Qb = g.Qb;
     c.Ma = g.Ma;
     c.Mb = g.Mb;
     c.rq = R.skip_rq;   // below 2^16 / qmax: the skip never exceeds nmax
-    c.dS = g.ds * g.Ss;
-    c.Sa = g.Sa;
-    c.Sb = g.Sb;
+    if (kBrick) {
+        // adding c * 2^32 changes neither the fraction nor the ambiguity test
+        c.off = ((long long)g.ca << 32) + g.off;
+        c.offb = ((long long)g.cb << 32) + g.off;
+        c.cs = g.cs;
+        c.ds = g.ds;
+        const int s = R.count_axis;
+        c.bs_s = brick_stride(s, v);
+        c.bs_a = brick_stride(g.ia, v);
+        c.bs_b = brick_stride(g.ib, v);
+        c.sh_s = 4 - 2 * s;
+        c.sh_a = 4 - 2 * g.ia;
+        c.sh_b = 4 - 2 * g.ib;
+    } else {
+        c.pk = fld + base;
+        c.off = g.off;
+        c.dS = g.ds * g.Ss;
+        c.Sa = g.Sa;
+        c.Sb = g.Sb;
+    }
     c.lim = lim;
     c.prev = m.prev;
     c.nseg = m.nseg;
@@ -426,11 +470,16 @@ __device__ __forceinline__ void chain_init(FieldChain &c, const FaceRule &R, con
 }
 
 // field byte of the chain's current increment
+template <bool kBrick>
 __device__ __forceinline__ uint32_t chain_load(const FieldChain &c, int cz, int cy, int cx, const Vol &v)
 {
-    const long long ea = c.off + (long long)c.i * c.Qa, eb = c.off + (long long)c.i * c.Qb;
+    const long long ea = c.off + (long long)c.i * c.Qa;
+    const long long eb = (kBrick ? c.offb : c.off) + (long long)c.i * c.Qb;
     if (((uint32_t)ea + c.Ma < 2u * c.Ma) | ((uint32_t)eb + c.Mb < 2u * c.Mb))
-        return exact_byte(*c.R, cz, cy, cx, c.i, v, c.fld);
+        return exact_byte(*c.R, cz, cy, cx, c.i, v, c.fld, kBrick);
+    if (kBrick)
+        return __ldg(c.fld + (brick_term(c.cs + c.i * c.ds, c.bs_s, c.sh_s) + brick_term((int)(ea >> 32), c.bs_a, c.sh_a) +
+                              brick_term((int)(eb >> 32), c.bs_b, c.sh_b)));
     return __ldg(c.pk + (c.i * c.dS + (int)(ea >> 32) * c.Sa + (int)(eb >> 32) * c.Sb));
 }
 
@@ -468,16 +517,17 @@ __device__ __forceinline__ void chain_done(const FieldChain &c, March &m)
 // The march of one lane on its field.  dlast: |displacement| of the last
 // accepted increment on the two non-step axes (a | b << 16), when its
 // fixed-point position is not near a rounding boundary; else -1.
+template <bool kBrick>
 __device__ __forceinline__ void field_march(const FaceRule &R, const LegGeom &g, int cz, int cy, int cx,
                                             const Vol &v, const uint8_t *fld, int base, int lim, uint32_t b0,
                                             March &m, bool &stopped, uint16_t *seg, int &dlast)
 {
     FieldChain c;
-    chain_init(c, R, g, fld, base, lim, b0, m);
+    chain_init<kBrick>(c, R, g, fld, base, lim, b0, m, v);
     while (c.on)
-        chain_step(c, chain_load(c, cz, cy, cx, v), seg, stopped);
+        chain_step(c, chain_load<kBrick>(c, cz, cy, cx, v), seg, stopped);
     chain_done(c, m);
-    const long long ea = c.off + (long long)c.last * c.Qa, eb = c.off + (long long)c.last * c.Qb;
+    const long long ea = g.off + (long long)c.last * g.Qa, eb = g.off + (long long)c.last * g.Qb;
     const bool amb = ((uint32_t)ea + c.Ma < 2u * c.Ma) | ((uint32_t)eb + c.Mb < 2u * c.Mb);
     dlast = amb ? -1 : (abs((int)(ea >> 32)) | abs((int)(eb >> 32)) << 16);
 }
@@ -596,7 +646,7 @@ struct LegState {
 
 // cube_face and the march set-up of one leg (warp-synchronous).  With kField
 // the lane's field march runs here too.
-template <bool kDetail, bool kField>
+template <bool kDetail, bool kField, bool kBrick>
 __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx, bool valid,
                                           const Vol &v, int full, uint16_t *seg, LegResult &out, LegState &S)
 {
@@ -666,14 +716,14 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
             if (kField) {
                 // per lane, no warp synchronisation: the field march
                 const uint8_t *fld = v.field + R.octant * v.field_stride;
-                b0 = __ldg(fld + base);
+                b0 = __ldg(fld + (kBrick ? brick_offset(cz, cy, cx, v.bsy, v.bsz) : base));
                 if ((b0 & 7u) == 0) {
                     stopped = true;
                 } else {
                     m.prev = (int)(b0 & 7u);
                     live = lim > 1;
                     if (live)
-                        field_march(R, g, cz, cy, cx, v, fld, base, lim, b0, m, stopped, seg, dlast);
+                        field_march<kBrick>(R, g, cz, cy, cx, v, fld, base, lim, b0, m, stopped, seg, dlast);
                 }
             } else {
                 const int lab0 = __ldg(v.p + base);
@@ -967,14 +1017,14 @@ __device__ __forceinline__ void leg_finish(const FaceRule *rules, int cz, int cy
 // kF32: the per-class lengths in FP32 (for A_h, which needs 1e-6; the march
 // itself, and hence the visited voxels, segments and len_path_2, is the same);
 // otherwise FP64 in the reference's order (bit-exact lengths).
-template <bool kDetail, bool kF32 = false, bool kField = false>
+template <bool kDetail, bool kF32 = false, bool kField = false, bool kBrick = false>
 __device__ __forceinline__ void trace_leg(const LegHead &h, const FaceRule *rules, int cz, int cy, int cx,
                                           bool valid, const Vol &v, int full, const double *voxel,
                                           const double *sq, int sq_stride, const double *qtab, uint16_t *seg,
                                           LegResult &out, const float *voxelf = nullptr)
 {
     LegState S;
-    leg_setup<kDetail, kField>(h, rules, cz, cy, cx, valid, v, full, seg, out, S);
+    leg_setup<kDetail, kField, kBrick>(h, rules, cz, cy, cx, valid, v, full, seg, out, S);
     if (!kField)
         leg_coop(rules, cz, cy, cx, v, seg, S);
     leg_finish<kDetail, kF32>(rules, cz, cy, cx, v, full, voxel, sq, sq_stride, qtab, seg, S, out, voxelf);
@@ -1041,7 +1091,7 @@ __device__ __forceinline__ void finish_item(float s, float c, const SampleDesc &
     }
 }
 
-template <int kMinBlocks, bool kField>
+template <int kMinBlocks, bool kField, bool kBrick = false>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const SampleDesc *__restrict__ descs,
                                                                         int n_desc, long long total_items,
                                                                         unsigned long long *__restrict__ work_counter)
@@ -1063,9 +1113,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
             break;
         const int si = find_sample(descs, n_desc, item);
         const SampleDesc &D = descs[si];
-        if (kField && !D.field) {
-            // a field variant launched over a sample without its field: an
-            // error status, no reads
+        if (kField && (!D.field || (D.brick_sz != 0) != kBrick)) {
+            // a field variant launched over a sample without its field (or
+            // with the other layout): an error status, no reads
             if (lane == 0)
                 atomicOr(D.status, 1 << kErrArgs);
             continue;
@@ -1083,7 +1133,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
         }
         __syncwarp();
 
-        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field, D.field_stride};
+        const Vol v{D.vol, D.dim[0], D.dim[1], D.dim[2], D.field, D.field_stride, D.brick_sy, D.brick_sz};
         float s = 0.0f, c = 0.0f;
         int bad = kOk;
         unsigned nsteps = 0;
@@ -1097,7 +1147,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
 #pragma unroll 1
             for (int leg = 0; leg < 2; leg++) {
                 LegResult a;
-                trace_leg<false, true, kField>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v,
+                trace_leg<false, true, kField, kBrick>(tab.head[leg], tab.rule[leg], cv.x, cv.y, cv.z, valid, v,
                                        D.full_iteration, D.voxel, D.sq, D.sq_stride, D.qtab, seg + tid, a,
                                        D.voxelf);
                 bad |= a.status;
@@ -1292,6 +1342,35 @@ __device__ __noinline__ int ib_leg(const LegHead &h, const FaceRule *rules, int 
     L[2] = cr_l;
     L[3] = bu_l;
     return kOk;
+}
+
+// ib_single_gridding's value (AnACor/src/ray_tracing.c:427-481) for n voxels
+// and one direction (leg 1 of `dir`): the diffracted leg's lengths by
+// iterative bisection, then cal_rate's exponent with a zero incident leg,
+// sum_m mu_m (0 + L_m) left to right.  vox_mu = voxel[3], mu[4].
+__global__ void __launch_bounds__(kBlock) ib_direction_kernel(const ReflTable *__restrict__ dir, const int8_t *vol,
+                                                              int dz, int dy, int dx, const short4 *coords, int n,
+                                                              const double *vox_mu, int num_cls, double *out,
+                                                              int *status)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n)
+        return;
+    const short4 cv = coords[k];
+    const Vol v{vol, dz, dy, dx};
+    double L[4];
+    const int st = ib_leg(dir->head[1], dir->rule[1], cv.x, cv.y, cv.z, v, num_cls, vox_mu, L);
+    status[k] = st;
+    if (st) {
+        out[k] = 0.0;
+        return;
+    }
+    const double *mu = vox_mu + 3;
+    double a = __dmul_rn(mu[0], __dadd_rn(0.0, L[0]));
+    a = __dadd_rn(a, __dmul_rn(mu[1], __dadd_rn(0.0, L[1])));
+    a = __dadd_rn(a, __dmul_rn(mu[2], __dadd_rn(0.0, L[2])));
+    a = __dadd_rn(a, __dmul_rn(mu[3], __dadd_rn(0.0, L[3])));
+    out[k] = a;
 }
 
 // ib_test over every work item: as absorption_kernel, with bisection paths.
@@ -1561,16 +1640,21 @@ cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long t
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess)
         return e;
-#define ANACOR_LAUNCH(B, F) absorption_kernel<B, F><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter)
+#define ANACOR_LAUNCH(B, F, K) \
+    absorption_kernel<B, F, K><<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter)
     switch (variant > 0 ? variant : absorption_variant()) {
-    case 1: ANACOR_LAUNCH(1, false); break;
-    case 3: ANACOR_LAUNCH(3, false); break;
-    case 4: ANACOR_LAUNCH(4, false); break;
-    case 5: ANACOR_LAUNCH(1, true); break;
-    case 6: ANACOR_LAUNCH(2, true); break;
-    case 7: ANACOR_LAUNCH(3, true); break;
-    case 8: ANACOR_LAUNCH(4, true); break;
-    default: ANACOR_LAUNCH(2, false); break;
+    case 1: ANACOR_LAUNCH(1, false, false); break;
+    case 3: ANACOR_LAUNCH(3, false, false); break;
+    case 4: ANACOR_LAUNCH(4, false, false); break;
+    case 5: ANACOR_LAUNCH(1, true, false); break;
+    case 6: ANACOR_LAUNCH(2, true, false); break;
+    case 7: ANACOR_LAUNCH(3, true, false); break;
+    case 8: ANACOR_LAUNCH(4, true, false); break;
+    case 9: ANACOR_LAUNCH(1, true, true); break;
+    case 10: ANACOR_LAUNCH(2, true, true); break;
+    case 11: ANACOR_LAUNCH(3, true, true); break;
+    case 12: ANACOR_LAUNCH(4, true, true); break;
+    default: ANACOR_LAUNCH(2, false, false); break;
     }
 #undef ANACOR_LAUNCH
     return cudaGetLastError();
@@ -1598,6 +1682,18 @@ cudaError_t launch_bisection(const SampleDesc *d_descs, int n_desc, long long to
     if (e != cudaSuccess)
         return e;
     bisection_kernel<<<grid, kBlock, 0, st>>>(d_descs, n_desc, total_items, d_counter, num_cls);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ib_direction(const ReflTable *d_dir, const int8_t *d_vol, const int *dims, const short4 *d_coords,
+                                int n, const double *d_vox_mu, int num_cls, double *d_out, int *d_status,
+                                cudaStream_t st)
+{
+    if (n <= 0)
+        return cudaSuccess;
+    ib_direction_kernel<<<(n + kBlock - 1) / kBlock, kBlock, 0, st>>>(d_dir, d_vol, dims[0], dims[1], dims[2],
+                                                                      d_coords, n, d_vox_mu, num_cls, d_out,
+                                                                      d_status);
     return cudaGetLastError();
 }
 
@@ -1683,16 +1779,21 @@ int absorption_set_carveout(int pct)
 int absorption_occupancy(int *blocks_per_sm, int variant)
 {
     cudaError_t e;
-#define ANACOR_OCC(B, F) cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<B, F>, kBlock, 0)
+#define ANACOR_OCC(B, F, K) \
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, absorption_kernel<B, F, K>, kBlock, 0)
     switch (variant > 0 ? variant : absorption_variant()) {
-    case 1: e = ANACOR_OCC(1, false); break;
-    case 3: e = ANACOR_OCC(3, false); break;
-    case 4: e = ANACOR_OCC(4, false); break;
-    case 5: e = ANACOR_OCC(1, true); break;
-    case 6: e = ANACOR_OCC(2, true); break;
-    case 7: e = ANACOR_OCC(3, true); break;
-    case 8: e = ANACOR_OCC(4, true); break;
-    default: e = ANACOR_OCC(2, false); break;
+    case 1: e = ANACOR_OCC(1, false, false); break;
+    case 3: e = ANACOR_OCC(3, false, false); break;
+    case 4: e = ANACOR_OCC(4, false, false); break;
+    case 5: e = ANACOR_OCC(1, true, false); break;
+    case 6: e = ANACOR_OCC(2, true, false); break;
+    case 7: e = ANACOR_OCC(3, true, false); break;
+    case 8: e = ANACOR_OCC(4, true, false); break;
+    case 9: e = ANACOR_OCC(1, true, true); break;
+    case 10: e = ANACOR_OCC(2, true, true); break;
+    case 11: e = ANACOR_OCC(3, true, true); break;
+    case 12: e = ANACOR_OCC(4, true, true); break;
+    default: e = ANACOR_OCC(2, false, false); break;
     }
 #undef ANACOR_OCC
     return e == cudaSuccess ? kOk : kErrCuda;

@@ -44,8 +44,10 @@ struct SampleDesc {
     int sq_stride;
     const double *qtab;     // optional quotient table covering den <= max(dim)
     long long work_begin;   // first global work item of this sample
-    const uint8_t *field;   // label | distance << 3 (launch_distance_field); required by variants 5..8
-    long long field_stride; // 0: one centred field; volume size: 8 octant fields (launch_octant_fields)
+    const uint8_t *field;   // label | distance << 3 (launch_distance_field); required by variants 5..12
+    long long field_stride; // 0: one centred field; else 8 octant fields this far apart (launch_octant_fields)
+    int brick_sy, brick_sz; // 0: linear fields; else 4^3-bricked (launch_brick_fields), byte strides of a
+                            // brick step in y and z; required by variants 9..12
     const int *order;       // optional [n_refl]: the k-th reflection processed (octant-sorted), else k
 };
 
@@ -109,9 +111,10 @@ int absorption_block_threads();
 int block_guard_selftest(int threads, int *status_out);
 int absorption_set_carveout(int pct);
 // Kernel variants: 1..4 the cooperative march with a register budget for
-// 1..4 CTAs per SM; 5..8 the same budgets with the distance-field march
-// (every sample needs its `field`).
-constexpr int kVariants = 8;
+// 1..4 CTAs per SM; 5..8 the same budgets with the distance-field march on
+// linear fields; 9..12 on 4^3-bricked fields (every sample needs its `field`
+// in the variant's layout).
+constexpr int kVariants = 12;
 // CTAs per SM of a variant (0 = the process default)
 int absorption_occupancy(int *blocks_per_sm, int variant = 0);
 // the process-default register-budget variant (CTAs per SM it targets)
@@ -147,6 +150,14 @@ cudaError_t launch_distance_field(const int8_t *d_vol, const int *dims, uint8_t 
 // d_out holds 8 volumes, d_tmp 6.
 cudaError_t launch_octant_fields(const int8_t *d_vol, const int *dims, uint8_t *d_out, uint8_t *d_tmp, int *d_bad,
                                  cudaStream_t st);
+// Bricked copies of `n_fields` linear fields (each dims[0]*dims[1]*dims[2]
+// bytes, consecutive): 4x4x4 bricks of 64 bytes in (z, y, x) brick order,
+// bytes (z, y, x) inside a brick, padding bytes 0.  Each copy holds
+// brick_field_bytes(dims) bytes; brick_strides gives the y and z brick steps.
+size_t brick_field_bytes(const int *dims);
+void brick_strides(const int *dims, int *sy, int *sz);
+cudaError_t launch_brick_fields(const uint8_t *d_lin, const int *dims, int n_fields, uint8_t *d_out,
+                                cudaStream_t st);
 // Persistent launch over every work item of `n_desc` samples; `grid` CTAs
 // take items from `d_counter` (reset inside the launch sequence).
 cudaError_t launch_absorption(const SampleDesc *d_descs, int n_desc, long long total_items,
@@ -160,6 +171,12 @@ cudaError_t launch_leg_detail(const ReflTable *d_tab, const int8_t *d_vol, const
 cudaError_t launch_bisection(const SampleDesc *d_descs, int n_desc, long long total_items,
                              unsigned long long *d_counter, int grid, int num_cls, cudaStream_t st);
 int bisection_occupancy(int *blocks_per_sm);
+// ib_single_gridding for n voxels of one direction (leg 1 of d_dir):
+// d_out[k] = sum_m mu_m (0 + L_m) with the bisection lengths (exp is left to
+// the caller), d_status[k] its status; d_vox_mu = voxel[3], mu[4].
+cudaError_t launch_ib_direction(const ReflTable *d_dir, const int8_t *d_vol, const int *dims, const short4 *d_coords,
+                                int n, const double *d_vox_mu, int num_cls, double *d_out, int *d_status,
+                                cudaStream_t st);
 // Persistent launch over n_dirs * tiles work items of the map.
 cudaError_t launch_gridding_map(const MapDesc *d_desc, long long total_items, unsigned long long *d_counter, int grid,
                                 cudaStream_t st, bool field = false);

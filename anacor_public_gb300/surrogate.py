@@ -141,6 +141,11 @@ class Surrogate:
             return mean[:n], spread[:n], mem[:, :n]
         return mean[:n], spread[:n]
 
+    def set_inference(self, fused: bool = True):
+        """Fused (one persistent kernel, activations on chip; the default) or
+        layer-by-layer inference; the same numbers either way."""
+        _lib.check(self._L.anacor_surrogate_set_inference(self._h, 1 if fused else 0), self._L)
+
     def predict_device(self, d_x7: int, n: int, d_mean: int, d_spread: int, stream: int | None = None,
                        d_members: int | None = None):
         """Enqueue inference on device buffers (raw pointers) on `stream`."""

@@ -139,8 +139,8 @@ class Plan:
     def configure(self, variant: int = 0, tile: int = 0, order: int = -1):
         """Execution parameters.  variant: 1..4 the warp-cooperative march
         compiled for 1..4 CTAs per SM, 5..8 the march on the chessboard distance
-        field, 9..12 on the 8 octant fields (both need labels in 0..7), 0 the
-        process default; tile: voxels per work item (0 unchanged); order: voxel
+        field, 9..12 on the 8 octant fields, 13..16 on the octant fields stored
+        in 4x4x4 bricks (fields need labels in 0..7), 0 the process default; tile: voxels per work item (0 unchanged); order: voxel
         order (0 the caller's, 1 Morton, 2..7 blocked, -1 unchanged).  Results
         do not depend on them beyond the FP32 summation order of A_h."""
         _lib.check(self._L.anacor_plan_configure(self._h, int(variant), int(tile), int(order)), self._L)
@@ -188,6 +188,10 @@ class Batch:
         self._h = ct.c_void_p(h)
 
     def configure(self, variant: int = 0):
+        """Variant of the whole launch (as Plan.configure): 1..4 every sample
+        on the cooperative march, 5..16 every sample on its field of that kind
+        (one launch; samples whose labels allow no field run in a second,
+        cooperative one)."""
         _lib.check(self._L.anacor_batch_configure(self._h, int(variant)), self._L)
 
     def autotune(self, sample_refl: int = 0):
@@ -231,6 +235,47 @@ def batch_run(plans, stream: int | None = None):
     L = _lib.load()
     arr = (ct.c_void_p * len(plans))(*[p._h.value for p in plans])
     _lib.check(L.anacor_batch_run(arr, len(plans), ct.c_void_p(stream or 0)), L)
+
+
+def choose_stride(label, voxel, mu, s1, omega, xray, omega_axis, F, strides=(2, 4, 8), tol: float = 1e-3,
+                  sample_refl: int = 64, crystal_code: int = 3) -> dict:
+    """Crystal-voxel sampling stride of a sample, chosen by what it costs in A_h.
+
+    The stride changes the answer, not only the speed, so it is chosen
+    against the every-voxel result: on the first `sample_refl` reflections
+    each candidate stride (the z, y, x multiples-of-stride lattice, sampled
+    on the GPU) is run and compared with stride 1; the largest stride whose
+    maximum relative deviation stays within `tol` wins (1 when none does).
+    Returns {"stride", "tol", "candidates": {stride: {"voxels", "ms_per_refl",
+    "median_dev", "max_dev"}}}."""
+    import time
+    k = min(int(sample_refl), len(omega))
+    s1 = _c(s1, np.float64).reshape(-1, 3)[:k]
+    omega = _c(omega, np.float64)[:k]
+    res, base = {}, None
+    for st in (1,) + tuple(int(x) for x in strides):
+        p = Plan.from_volume(label, voxel, mu, crystal_code, method="stride" if st > 1 else "all", stride=st)
+        try:
+            if p.n_vox == 0:
+                continue
+            p.set_reflections(s1, omega, xray, omega_axis, F)
+            p.run()
+            a = p.result()
+            t0 = time.perf_counter()
+            p.run()
+            a = p.result()
+            ms = (time.perf_counter() - t0) * 1e3 / max(k, 1)
+        finally:
+            p.close()
+        if st == 1:
+            base = a
+            res[1] = {"voxels": int(p.n_vox), "ms_per_refl": ms, "median_dev": 0.0, "max_dev": 0.0}
+            continue
+        dev = np.abs(a - base) / np.abs(base)
+        res[st] = {"voxels": int(p.n_vox), "ms_per_refl": ms, "median_dev": float(np.median(dev)),
+                   "max_dev": float(np.max(dev))}
+    ok = [st for st, r in res.items() if st > 1 and r["max_dev"] <= tol]
+    return {"stride": max(ok) if ok else 1, "tol": float(tol), "candidates": res}
 
 
 def sample_voxels(label, crystal_code: int = 3, method: str = "all", sampling_size: int = 5000,

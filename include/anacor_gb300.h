@@ -146,7 +146,10 @@ int anacor_bisection(const int8_t *label, const int64_t *shape, const int64_t *c
  * march (steps over increments that a chessboard distance field proves to
  * keep the label; needs labels in 0..7, else kErrUnsupported), 9..12 the
  * same on the 8 octant fields (each leg reads the field of its direction's
- * octant), 0 = process default; tile = voxels per work item
+ * octant), 13..16 the same on a copy of the octant fields stored in 4x4x4
+ * bricks of 64 bytes (a ray's next step along any axis mostly stays in the
+ * 32-byte sector of its last load), 0 = process default; tile = voxels per
+ * work item
  * (>= 128, 0 = unchanged); order = voxel order of the packed list: 0 the
  * caller's, 1 Morton (Z-order) of (z, y, x), 2..7 blocked (Morton order of
  * blocks of 1x2x16, 1x4x8, 2x4x32, 4x8x64, 4x16x32 or 8x16x128 voxels, row
@@ -180,7 +183,14 @@ int anacor_batch_run(anacor_plan *const *plans, int n_plans, void *stream);
  * anacor_batch_configure to refresh it. */
 typedef struct anacor_batch anacor_batch;
 anacor_batch *anacor_batch_create(anacor_plan *const *plans, int n_plans);
+/* variant (as for anacor_plan_configure) of the whole launch: 1..4 every
+ * sample on the cooperative march; 5..16 every sample on its field of that
+ * kind (built here when missing), one launch; each sample keeps its own tile
+ * and voxel order. */
 int anacor_batch_configure(anacor_batch *b, int variant);
+/* Each plan's tile and voxel order by anacor_plan_autotune, then the
+ * launch variant: the fastest of every register budget of the cooperative
+ * march and of each field kind the samples allow, timed as whole launches. */
 int anacor_batch_autotune(anacor_batch *b, int64_t sample_refl);
 int anacor_batch_launch(anacor_batch *b, void *stream);
 int anacor_batch_capture(anacor_batch *b, void *stream);
@@ -188,10 +198,9 @@ int anacor_batch_replay(anacor_batch *b, void *stream);
 /* synchronise `stream` and check every plan's device status word */
 int anacor_batch_wait(anacor_batch *b, void *stream);
 int anacor_batch_info(const anacor_batch *b, int *grid, long long *items, int *variant);
-/* Kernel launches per batch run: 1, or 2 under a distance-field variant
- * (5..8) when the batch mixes samples that march on their field (their plan
- * configured to a field variant, e.g. by the autotuner) with samples that do
- * not: those run first in the cooperative kernel of the same register budget. */
+/* Kernel launches per batch run: 1, or 2 under a field variant when some
+ * sample's labels allow no field (labels outside 0..7): those samples run
+ * first in the cooperative kernel of the same register budget. */
 int anacor_batch_kernels(const anacor_batch *b);
 void anacor_batch_destroy(anacor_batch *b);
 
@@ -305,8 +314,12 @@ double ray_tracing_single_gridding(int64_t *coord, const double *rotated_s1, dou
                                    double *voxel_size, double *coefficients, int8_t ***label_list, int64_t *shape,
                                    int full_iteration, int index, int IsExp);
 /* Drop-in for AnACor/src/ray_tracing.c:427-482 (bound at
- * utils_gridding.py:120-134): the bisection method is not implemented; NaN
- * with ANACOR_ERR_UNSUPPORTED. */
+ * utils_gridding.py:120-134): the same value with the diffracted leg's
+ * lengths found by iterative bisection (resolution 1.0; num_cls > 3 also
+ * searches bubble boundaries) on the GPU; exp(-sum) taken on the host when
+ * IsExp.  NaN with ANACOR_ERR_ASSERT where the reference asserts, and
+ * ANACOR_ERR_ARGS where a search leaves the volume (undefined in the
+ * reference).  Shares the cached volume of ray_tracing_single_gridding. */
 double ib_single_gridding(int64_t *coord, const double *rotated_s1, double theta, double phi, double *voxel_size,
                           double *coefficients, int8_t ***label_list, int64_t *shape, int full_iteration, int index,
                           int num_cls, int IsExp);
@@ -375,6 +388,13 @@ int anacor_surrogate_predict(anacor_surrogate *s, const float *x7, int64_t n, fl
                              float *members_out);
 int anacor_surrogate_predict_device(anacor_surrogate *s, const float *d_x7, int64_t n, float *d_mean,
                                     float *d_spread, float *d_members, void *stream);
+/* How inference runs: fused = 1 (the default) one persistent kernel per call
+ * that keeps a 128-row tile's features and activations in shared memory and
+ * its accumulator in tensor memory through all four layers and the head of
+ * every member (weights streamed by bulk copies); 0 layer by layer, each
+ * layer a tensor-core GEMM whose activations go through device memory.  Both
+ * give the same numbers. */
+int anacor_surrogate_set_inference(anacor_surrogate *s, int fused);
 /* flags[i] bit 0: row i is in the seeded random audit sample (probability
  * audit_fraction); bit 1: spread[i] > spread_threshold or not finite */
 int anacor_surrogate_audit_flags(const float *d_spread, int64_t n, uint32_t seed, double audit_fraction,

@@ -754,3 +754,34 @@ int oracle_ib(const int64_t *coords, int64_t n, const double *s1_rot, const doub
     *out = sum / n;
     return ORC_OK;
 }
+
+/* ib_single_gridding (AnACor/src/ray_tracing.c:427-482) for n voxels and one
+ * direction: the given theta/phi must be the vector's to 1e-6 (the reference
+ * asserts), the diffracted leg's exit face from cube_face, its lengths by
+ * iterative bisection with those angles, then cal_rate with a zero incident
+ * leg.  out[k] per voxel. */
+int oracle_ib_gridding(const int64_t *coords, int64_t n, const double *s1_rot, double theta, double phi,
+                       const double *voxel, const double *mu, const int8_t *vol, const int64_t *shape, int num_cls,
+                       int is_exp, double *out)
+{
+    if (n <= 0 || check_coords(coords, n, shape))
+        return ORC_ERR_ARGS;
+    double th, ph, d_out[3];
+    oracle_theta_phi(s1_rot, 0, &th, &ph);
+    if (!(fabs(th - theta) < 1e-6) || !(fabs(ph - phi) < 1e-6))
+        return ORC_ERR_ASSERT;
+    oracle_myframe(s1_rot, d_out);
+    const double zero[4] = {0, 0, 0, 0};
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t *c = coords + 3 * k;
+        const int64_t f = oracle_cube_face(c, d_out, shape, 0);
+        if (!f)
+            return ORC_ERR_FACE;
+        double l2[4];
+        const int st = ib_leg(c, f, theta, phi, vol, shape, num_cls, voxel, l2);
+        if (st)
+            return st;
+        out[k] = rate(zero, l2, mu, is_exp);
+    }
+    return ORC_OK;
+}

@@ -67,7 +67,22 @@ class Oracle:
                                   ct.c_void_p]
         lib.oracle_cube_face.restype = ct.c_int64
         lib.oracle_cube_face.argtypes = [_i64p, _f64p, _i64p, ct.c_int]
+        lib.oracle_ib_gridding.restype = ct.c_int
+        lib.oracle_ib_gridding.argtypes = [_i64p, ct.c_int64, _f64p, ct.c_double, ct.c_double, _f64p, _f64p, _i8p,
+                                           _i64p, ct.c_int, ct.c_int, _f64p]
         self.lib = lib
+
+    def ib_gridding(self, coords, rotated_s1, theta, phi, voxel, mu, label, num_cls=4, is_exp=0) -> np.ndarray:
+        """ib_single_gridding's value for every voxel of `coords` and one
+        direction: [n] doubles.  Raises on a status."""
+        coords = _c(coords, np.int64).reshape(-1, 3)
+        out = np.zeros(len(coords))
+        st = self.lib.oracle_ib_gridding(coords, len(coords), _c(rotated_s1, np.float64), float(theta), float(phi),
+                                         _c(voxel, np.float64), _c(mu, np.float64), _c(label, np.int8),
+                                         np.array(label.shape, dtype=np.int64), int(num_cls), int(is_exp), out)
+        if st:
+            raise RuntimeError(f"oracle_ib_gridding: {STATUS.get(st, st)}")
+        return out
 
     def overall(self, s, threads: int = 0, full_iteration: int = 0, is_exp: int = 1) -> np.ndarray:
         out = np.zeros(s.n_refl, dtype=np.float64)
@@ -211,6 +226,10 @@ class Reference:
         lib.ray_tracing_single_gridding.argtypes = [_i64p, _f64p, ct.c_double, ct.c_double, _f64p, _f64p,
                                                     ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8))), _i64p, ct.c_int,
                                                     ct.c_int, ct.c_int]
+        lib.ib_single_gridding.restype = ct.c_double
+        lib.ib_single_gridding.argtypes = [_i64p, _f64p, ct.c_double, ct.c_double, _f64p, _f64p,
+                                           ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8))), _i64p, ct.c_int, ct.c_int,
+                                           ct.c_int, ct.c_int]
         lib.ib_test.restype = ct.c_double
         lib.ib_test.argtypes = [_i64p, ct.c_int64, _f64p, _f64p, _f64p, _f64p,
                                 ct.POINTER(ct.POINTER(ct.POINTER(ct.c_int8))), _i64p, ct.c_int, ct.c_int64,
@@ -241,6 +260,22 @@ class Reference:
             out[k] = self.lib.ray_tracing_single_gridding(np.ascontiguousarray(c), s.copy(), float(theta),
                                                           float(phi), _c(voxel, np.float64), _c(mu, np.float64),
                                                           tab, shape, full_iteration, 0, is_exp)
+        del keep
+        return out
+
+    def ib_single_gridding(self, coords, rotated_s1, theta, phi, voxel, mu, label, num_cls=4, is_exp=0):
+        """ib_single_gridding (AnACor/src/ray_tracing.c:427-482) for every
+        voxel of `coords` and one direction: [n] doubles."""
+        label = _c(label, np.int8)
+        tab, keep = row_table(label)
+        shape = np.array(label.shape, dtype=np.int64)
+        out = np.empty(len(coords))
+        s = _c(rotated_s1, np.float64)
+        with silence_stdout():
+            for k, c in enumerate(_c(coords, np.int64)):
+                out[k] = self.lib.ib_single_gridding(np.ascontiguousarray(c), s.copy(), float(theta), float(phi),
+                                                     _c(voxel, np.float64), _c(mu, np.float64), tab, shape, 0, 0,
+                                                     int(num_cls), is_exp)
         del keep
         return out
 

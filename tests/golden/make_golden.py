@@ -193,6 +193,26 @@ def bisection_and_gridding(ref):
     np.savez_compressed(os.path.join(HERE, "small_grid.npz"), dirs=dirs, s1=s1[dirs], angles=np.array(angles),
                         coords=vox, value=np.array(vals))
     print("ib", ib[4][:3], "grid", vals[0][:3])
+    ib_grid_fixture(ref)
+
+
+def ib_grid_fixture(ref):
+    """ib_single_gridding values of 64 voxels x 8 grid directions of a 36 x 18
+    grid, num_cls 4 and 3, exponent and exp (python make_golden.py --ib-grid)."""
+    from oracle import gridding_oracle as go
+    s = synth.small_sample()
+    s1, th, ph = go.directions(36, 18)
+    rng = np.random.default_rng(1)
+    dirs = np.sort(rng.choice(len(s1), 8, replace=False))
+    vox = np.ascontiguousarray(s.coords[np.sort(rng.choice(len(s.coords), 64, replace=False))])
+    out = {}
+    for ncls in (4, 3):
+        for ex in (0, 1):
+            out[f"v{ncls}_{ex}"] = np.array([ref.ib_single_gridding(vox, s1[d], th[d], ph[d], s.voxel, s.mu,
+                                                                    s.label, ncls, ex) for d in dirs])
+    np.savez_compressed(os.path.join(HERE, "small_ib_grid.npz"), dirs=dirs, s1=s1[dirs],
+                        angles=np.stack([th[dirs], ph[dirs]], 1), coords=vox, digest=sample_digest(s), **out)
+    print("ib grid", out["v4_0"][0][:3])
 
 
 def _legs(ref, s, k, coords):
@@ -249,6 +269,9 @@ def main():
         return
     if "--modes" in sys.argv:
         bisection_and_gridding(ref)
+        return
+    if "--ib-grid" in sys.argv:
+        ib_grid_fixture(ref)
         return
     if "--cylinder" in sys.argv:
         cylinder_kat(ref)

@@ -133,7 +133,7 @@ def want(sample, oracle):
     return oracle.overall(sample, threads=os.cpu_count() or 1)
 
 
-@pytest.mark.parametrize("variant", [5, 6, 7, 8, 9, 10, 11, 12])
+@pytest.mark.parametrize("variant", [5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16])
 @pytest.mark.parametrize("tile,order", [(512, 1), (2048, 0), (128, 3)])
 def test_field_variants_match_the_oracle_and_the_cooperative_march(sample, want, variant, tile, order):
     p = tracer.Plan.from_sample(sample)
@@ -150,7 +150,7 @@ def test_field_variants_match_the_oracle_and_the_cooperative_march(sample, want,
     p.close()
 
 
-@pytest.mark.parametrize("variant", [8, 12])
+@pytest.mark.parametrize("variant", [8, 12, 16])
 def test_field_march_beamline_vs_golden(golden_dir, variant):
     gold = np.load(os.path.join(golden_dir, "beamline_ah.npz"))["ah"]
     b = synth.beamline_sample(n_refl=12)
@@ -191,13 +191,16 @@ def test_field_march_on_wall_and_slab_volumes(oracle):
     v = blocky_volume((40, 44, 48), 7, labels=(1, 2, 4, 5, 6))   # codes 5..7 change no class
     v[14:26, 16:28, 18:30] = 3
     vols.append(v)
+    v = blocky_volume((37, 42, 29), 8, labels=(1, 2, 4))   # axes not multiples of the 4^3 bricks
+    v[12:25, 14:28, 9:20] = 3
+    vols.append(v)
     for vol in vols:
         coords = np.ascontiguousarray(np.argwhere(vol == 3).astype(np.int64))
         t = synth.Sample(label=vol, coords=coords, s1=s.s1, omega=s.omega, xray=s.xray, omega_axis=s.omega_axis,
                          F=s.F, voxel=s.voxel, mu=s.mu)
         ref = oracle.overall(t, threads=4)
         a4, n4 = _run(t, 4)
-        for v in (8, 12):
+        for v in (8, 12, 16):
             a8, n8 = _run(t, v)
             assert max_rel(a8, ref) <= RTOL
             assert np.array_equal(a8, a4) and n8 == n4
@@ -208,7 +211,7 @@ def test_field_variant_refused_for_wide_labels(sample):
     vol[0, 0, 0] = 12
     p = tracer.Plan(vol, sample.coords, sample.voxel, sample.mu)
     p.set_reflections(sample.s1[:8], sample.omega[:8], sample.xray, sample.omega_axis, sample.F)
-    for v in (8, 12):
+    for v in (8, 12, 16):
         with pytest.raises(_lib.AnacorError) as e:
             p.configure(v, 512, 1)
         assert e.value.status == K_UNSUPPORTED
@@ -217,7 +220,7 @@ def test_field_variant_refused_for_wide_labels(sample):
     p.close()
 
 
-def test_batch_splits_field_and_cooperative_samples(oracle):
+def test_batch_runs_samples_without_a_field_in_a_cooperative_launch(oracle):
     import torch
     samples = synth.batch_samples(n_samples=3, max_refl=16, dim_range=(64, 128))
     wide = samples[2].label.copy()
@@ -233,7 +236,7 @@ def test_batch_splits_field_and_cooperative_samples(oracle):
     b = tracer.Batch(plans)
     st = torch.cuda.Stream()
     got = {}
-    for v, kernels in ((8, 2), (4, 1), (7, 2)):
+    for v, kernels in ((8, 2), (4, 1), (7, 2), (16, 2), (11, 2)):
         b.configure(v)
         assert b.info()["kernels"] == kernels
         b.launch(st.cuda_stream)
@@ -259,7 +262,7 @@ def test_field_variants_with_full_iteration_and_no_exp(small, oracle):
     for full, ie in ((1, 1), (0, 0), (1, 0)):
         ref = oracle.overall(s, threads=os.cpu_count() or 1, full_iteration=full, is_exp=ie)
         got = {}
-        for v in (4, 8, 12):
+        for v in (4, 8, 12, 16):
             p = tracer.Plan(s.label, s.coords, s.voxel, s.mu, full_iteration=full, is_exp=ie)
             p.set_reflections(s.s1, s.omega, s.xray, s.omega_axis, s.F)
             p.configure(v, 512, 1)
@@ -267,4 +270,4 @@ def test_field_variants_with_full_iteration_and_no_exp(small, oracle):
             got[v] = p.result()
             p.close()
             assert max_rel(got[v], ref) <= RTOL, (full, ie, v)
-        assert np.array_equal(got[8], got[4]) and np.array_equal(got[12], got[4])
+        assert np.array_equal(got[8], got[4]) and np.array_equal(got[12], got[4]) and np.array_equal(got[16], got[4])

@@ -6,6 +6,7 @@ relative (FP32 exp after FP64 range reduction and a compensated FP32 mean,
 as for the plain kernel).
 """
 import ctypes as ct
+import os
 
 import numpy as np
 import pytest
@@ -134,9 +135,29 @@ def test_dropin_single_gridding(small):
     v = L.ray_tracing_single_gridding(np.ascontiguousarray(small.coords[0]), np.ascontiguousarray(s1[0]),
                                       th[0] + 0.1, ph[0], small.voxel, small.mu, tab, shape, 0, 0, 0)
     assert np.isnan(v) and L.anacor_last_status() == 2
-    v = L.ib_single_gridding(np.ascontiguousarray(small.coords[0]), np.ascontiguousarray(s1[0]), th[0], ph[0],
-                             small.voxel, small.mu, tab, shape, 0, 0, 4, 0)
-    assert np.isnan(v) and L.anacor_last_status() == 6
+    v = L.ib_single_gridding(np.ascontiguousarray(small.coords[0]), np.ascontiguousarray(s1[0]), th[0] + 0.1,
+                             ph[0], small.voxel, small.mu, tab, shape, 0, 0, 4, 0)
+    assert np.isnan(v) and L.anacor_last_status() == 2
+    del keep
+
+
+def test_dropin_ib_single_gridding_vs_reference_fixture(small, golden_dir):
+    """ib_single_gridding through the drop-in: bit for bit with the reference's
+    own values (64 voxels x 8 directions, num_cls 4 and 3, exponent and exp)."""
+    build.build()
+    L = _lib.load()
+    g = np.load(os.path.join(golden_dir, "small_ib_grid.npz"))
+    tab, keep = row_table(np.ascontiguousarray(small.label))
+    shape = np.array(small.label.shape, dtype=np.int64)
+    for ncls in (4, 3):
+        for ex in (0, 1):
+            want = g[f"v{ncls}_{ex}"]
+            for j in range(len(g["dirs"])):
+                th, ph = g["angles"][j]
+                for k, c in enumerate(g["coords"]):
+                    v = L.ib_single_gridding(np.ascontiguousarray(c), np.ascontiguousarray(g["s1"][j]), th, ph,
+                                             small.voxel, small.mu, tab, shape, 0, 0, ncls, ex)
+                    assert v == want[j, k], (ncls, ex, j, k, v, want[j, k], L.anacor_last_error())
     del keep
 
 

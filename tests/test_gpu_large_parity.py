@@ -14,8 +14,9 @@ their seeds and pinned by the fixtures' input digests:
 
 Tolerances: A_h within 1e-6 relative of the reference (FP64 throughout there);
 exit face, len_path_2, segment count, path end points and the four per-material
-lengths bit-identical; the three marches (warp-cooperative, centred distance
-field, octant fields) visit the same label steps (sum of len_path_2 equal).
+lengths bit-identical; the four marches (warp-cooperative, centred distance
+field, octant fields, octant fields in 4^3 bricks) visit the same label
+steps (sum of len_path_2 equal).
 """
 import os
 import sys
@@ -34,7 +35,8 @@ sys.path.insert(0, GOLDEN)
 from make_golden import sample_digest  # noqa: E402
 
 # one variant per march kind, at the 4-CTA and 2-CTA register budgets
-VARIANTS = {"cooperative": (4, 2), "centred field": (8, 6), "octant fields": (12, 10)}
+VARIANTS = {"cooperative": (4, 2), "centred field": (8, 6), "octant fields": (12, 10),
+            "bricked octant fields": (16, 14)}
 
 
 @pytest.fixture(scope="module")

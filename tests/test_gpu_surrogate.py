@@ -178,6 +178,30 @@ def test_predict_matches_oracle_forward(small, trained_small):
     assert np.allclose(spread, a.std(axis=0) / a.mean(axis=0), atol=1e-5)
 
 
+def test_fused_inference_matches_layered(small, trained_small):
+    """The fused kernel (features, four layers, head and ensemble statistics of
+    a 128-row tile on chip) against the layer-by-layer GEMM path on the same
+    rows, including a partial last tile: the same arithmetic, so the same
+    numbers (compared to 1e-6 relative; reported when bitwise equal)."""
+    model, _ = trained_small
+    rng = np.random.default_rng(5)
+    omega, s1 = synth.reflections(5000, rng, xray=small.xray)
+    x7 = surrogate.inputs(omega, s1, small.xray, small.omega_axis, small.F)
+    try:
+        model.set_inference(False)
+        m0, s0, e0 = model.predict(x7, members=True)
+        model.set_inference(True)
+        m1, s1_, e1 = model.predict(x7, members=True)
+    finally:
+        model.set_inference(True)
+    assert np.all(np.isfinite(m1)) and np.all(np.isfinite(s1_))
+    print(f"\nfused vs layered: mean bitwise {np.array_equal(m0, m1)}, members bitwise {np.array_equal(e0, e1)}, "
+          f"max rel diff mean {np.max(np.abs(m1 - m0) / np.abs(m0)):.2e}")
+    assert np.allclose(m1, m0, rtol=1e-6, atol=0)
+    assert np.allclose(e1, e0, rtol=1e-6, atol=1e-7)
+    assert np.allclose(s1_, s0, rtol=1e-4, atol=1e-8)
+
+
 def test_audited_absorption_small(small, trained_small):
     model, _ = trained_small
     rng = np.random.default_rng(99)

@@ -38,6 +38,34 @@ def test_oracle_map_value_matches_reference_fixture(small, oracle, fx):
         assert np.array_equal(a, g["value"][k])
 
 
+def test_oracle_ib_single_gridding_matches_reference_fixture(small, oracle, golden_dir):
+    g = np.load(os.path.join(golden_dir, "small_ib_grid.npz"))
+    from tests.golden.make_golden import sample_digest
+    assert str(g["digest"]) == sample_digest(small)
+    for ncls in (4, 3):
+        for ex in (0, 1):
+            got = np.array([oracle.ib_gridding(g["coords"], g["s1"][j], g["angles"][j, 0], g["angles"][j, 1],
+                                               small.voxel, small.mu, small.label, ncls, ex)
+                            for j in range(len(g["dirs"]))])
+            assert np.array_equal(got, g[f"v{ncls}_{ex}"]), (ncls, ex)
+
+
+def test_oracle_ib_single_gridding_reports_the_reference_assert(small, oracle):
+    s1, th, ph = go.directions(36, 18)
+    with pytest.raises(RuntimeError, match="assert"):
+        oracle.ib_gridding(small.coords[:4], s1[7], th[7] + 0.1, ph[7], small.voxel, small.mu, small.label)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference library not built (oracle/_ref)")
+def test_oracle_ib_single_gridding_live_other_directions(small, oracle):
+    r = Reference()
+    s1, th, ph = go.directions(24, 12)
+    vox = small.coords[::97]
+    for d in range(5, len(s1), 41):
+        assert np.array_equal(oracle.ib_gridding(vox, s1[d], th[d], ph[d], small.voxel, small.mu, small.label, 4, 1),
+                              r.ib_single_gridding(vox, s1[d], th[d], ph[d], small.voxel, small.mu, small.label, 4, 1))
+
+
 @pytest.mark.skipif(not os.path.exists(REF_SO), reason="reference library not built (oracle/_ref)")
 def test_oracle_bisection_live_other_seed():
     s = synth.small_sample(n_refl=40, seed=3)

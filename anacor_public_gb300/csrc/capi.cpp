@@ -803,10 +803,23 @@ int plan_configure(anacor_plan *p, int variant, int tile, int order)
 int plan_time(anacor_plan *p, int64_t k, int reps, float *ms)
 {
     const int64_t keep = p->n_refl;
+    cudaError_t e = cudaSuccess;
+    // the sample: k reflections spread evenly over the processing order (so
+    // every octant pair and the whole range of directions is in it), not the
+    // first k, which all share one pair of direction octants
+    const bool spread = k < keep && p->h_order.size() >= (size_t)keep;
+    if (spread) {
+        std::vector<int> sub((size_t)k);
+        for (int64_t j = 0; j < k; j++)
+            sub[(size_t)j] = p->h_order[(size_t)((j * keep) / k)];
+        if ((e = cudaMemcpyAsync(p->d_order, sub.data(), (size_t)k * sizeof(int), cudaMemcpyHostToDevice,
+                                 p->stream)) ||
+            (e = cudaStreamSynchronize(p->stream)))
+            return cuda_fail(e, "tuning sample");
+    }
     p->n_refl = k;
     int st = plan_upload_desc(p, nullptr);
     cudaEvent_t a = nullptr, b = nullptr;
-    cudaError_t e = cudaSuccess;
     if (!st && ((e = cudaEventCreate(&a)) || (e = cudaEventCreate(&b))))
         st = cuda_fail(e, "event");
     if (!st)
@@ -825,6 +838,10 @@ int plan_time(anacor_plan *p, int64_t k, int reps, float *ms)
     if (b)
         cudaEventDestroy(b);
     p->n_refl = keep;
+    if (spread && ((e = cudaMemcpyAsync(p->d_order, p->h_order.data(), (size_t)k * sizeof(int),
+                                        cudaMemcpyHostToDevice, p->stream)) ||
+                   (e = cudaStreamSynchronize(p->stream))))
+        return st ? st : cuda_fail(e, "processing order");
     const int st2 = plan_upload_desc(p, nullptr);
     return st ? st : st2;
 }
@@ -1705,10 +1722,12 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
     auto timed = [&](int variant, int tile, int order, float &out) -> int {
         if (int st = plan_configure(p, variant, tile, order))
             return st;
-        const long long slots = (long long)p->dev->sms * variant_occupancy(p->dev, variant);
-        int64_t k = (int64_t)((8 * slots + p->tiles - 1) / p->tiles);
-        if (sample_refl > 0)
-            k = std::max<int64_t>(k, sample_refl);
+        // about eight waves of warp work items, and at least 32 reflections
+        // (spread over all of them) so that the sample's directions are the
+        // workload's
+        const long long warps = (long long)p->dev->sms * variant_occupancy(p->dev, variant) * 8;
+        int64_t k = (int64_t)((8 * warps + p->tiles - 1) / p->tiles);
+        k = std::max<int64_t>(k, std::max<int64_t>(32, sample_refl));
         k = std::min<int64_t>(k, p->n_refl);
         out = 1e30f;
         for (int rep = 0; rep < 5; rep++) {
@@ -1716,6 +1735,8 @@ int anacor_plan_autotune(anacor_plan *p, int64_t sample_refl, float *best_ms)
             if (int st = plan_time(p, k, 1, &ms))
                 return st;
             out = std::min(out, ms * (float)p->n_refl / (float)k);
+            if (ms > 20.0f && rep >= 1)   // long runs: best of two is steady enough
+                break;
         }
         return kOk;
     };

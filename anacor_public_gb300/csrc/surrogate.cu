@@ -615,8 +615,9 @@ __global__ void audit_kernel(const float *__restrict__ spread, long long n, uint
 // one persistent kernel: the tile's Fourier features and each layer's
 // activations stay in shared memory, the accumulator in tensor memory, and
 // only the weights stream in (from L2: 1.7 MB for four members), as 32 KiB
-// K-chunks copied by the bulk-copy engine (cp.async.bulk) into a 3-stage ring.
-// One thread issues the tcgen05 MMAs; all eight warps run the epilogue (bias,
+// K-chunks copied by the bulk-copy engine (cp.async.bulk) into a 4-stage ring
+// kept three chunks ahead of the MMAs.
+// One thread issues the tcgen05 MMAs; all twelve warps run the epilogue (bias,
 // GELU, BF16 into the next layer's operand tile, or the head's dot product).
 // The arithmetic is the layered path's: same MMA sequence, the same epilogue
 // expressions and the head's and ensemble's summation orders, so the outputs
@@ -624,8 +625,8 @@ __global__ void audit_kernel(const float *__restrict__ spread, long long n, uint
 
 constexpr int kChunkBytes = kWidth * umma::kBK * 2;                    // one 256 x 64 BF16 weight chunk
 constexpr int kChunksPerMember = 1 + (kDepth - 1) * (kWidth / umma::kBK);  // 13
-constexpr int kInferStages = 3;
-constexpr int kInferThreads = 256;
+constexpr int kInferStages = 4;
+constexpr int kInferThreads = 384;   // 12 warps: three per TMEM lane quarter
 constexpr int kTileRows = umma::kBM;                                    // 128
 constexpr int kActChunk = kTileRows * umma::kBK * 2;                   // 16 KiB
 constexpr int kMemberConsts = kDepth * kWidth + kWidth + 2;             // biases, w5, b5, pad
@@ -633,10 +634,13 @@ constexpr int kGStride = 33;                                            // head 
 constexpr int kOffInferAct = kInferStages * kChunkBytes;
 constexpr int kOffInferX0 = kOffInferAct + (kWidth / umma::kBK) * kActChunk;
 constexpr int kOffInferC = kOffInferX0 + kActChunk;
-constexpr int kOffInferG = kOffInferC + ((kMemberConsts * 4 + 15) / 16) * 16;
-constexpr int kOffInferY = kOffInferG + kTileRows * kGStride * 4;
+constexpr int kOffInferY = kOffInferC + ((kMemberConsts * 4 + 15) / 16) * 16;
 constexpr int kInferSmem = kOffInferY + kMaxMembers * kTileRows * 4;
-static_assert(kInferSmem <= 227 * 1024, "fused inference shared memory");
+// the head's partial sums live in the activation tile, which the last
+// layer's MMAs have finished reading when the head writes them
+constexpr int kOffInferG = kOffInferAct;
+static_assert(kTileRows * kGStride * 4 <= (kWidth / umma::kBK) * kActChunk, "head partials fit the tile");
+static_assert(kInferSmem + 256 <= 227 * 1024, "fused inference shared memory");
 
 struct WeightPtrs {
     const bf16 *w[kDepth];
@@ -755,12 +759,14 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
             ok = issue(q_issue) && ok;
 
     const int rl = 32 * (warp & 3) + lane;     // this thread's row of the tile (TMEM lane)
-    const int cb = (warp >> 2) * (kWidth / 2);  // first of its 128 accumulator columns
+    // its accumulator columns: warps 0-3 take 0..95, 4-7 96..175, 8-11 176..255
+    const int cb = warp < 4 ? 0 : (warp < 8 ? 96 : 176);
+    const int ce = warp < 4 ? 96 : (warp < 8 ? 176 : kWidth);
     for (long long ti = 0; ti < my_tiles && ok; ti++) {
         const long long row0 = (blockIdx.x + ti * gridDim.x) * kTileRows;
         // Fourier features of the tile (features_kernel's expressions), BF16
         // into the layer-0 operand tile; rows past n are zeros
-        {
+        if (tid < 2 * kTileRows) {
             const int r = tid >> 1, h = tid & 1;
             const long long i = row0 + r;
             float sv[16], cv[16];
@@ -835,16 +841,17 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
                 umma::tc_fence_after();
                 const float *bias = cst + l * kWidth;
                 const float *w5 = cst + kDepth * kWidth;
-                for (int c0 = cb; c0 < cb + kWidth / 2; c0 += 16) {
+                for (int c0 = cb; c0 < ce; c0 += 16) {
                     float v[16];
                     umma::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c0, v);
 #pragma unroll
                     for (int q = 0; q < 16; q++)
                         v[q] = gelu(v[q] + bias[c0 + q]);
-                    __align__(16) bf16 t[16];
+                    __align__(16) __nv_bfloat162 t2[8];
 #pragma unroll
-                    for (int q = 0; q < 16; q++)
-                        t[q] = __float2bfloat16_rn(v[q]);
+                    for (int q = 0; q < 8; q++)
+                        t2[q] = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+                    const bf16 *t = reinterpret_cast<const bf16 *>(t2);
                     if (l < kDepth - 1) {
                         uint8_t *dst = Act + (c0 / umma::kBK) * kActChunk;
                         const int k = c0 % umma::kBK;

@@ -613,58 +613,113 @@ __global__ void audit_kernel(const float *__restrict__ spread, long long n, uint
 //
 // The four hidden layers and the head of every member for a 128-row tile in
 // one persistent kernel: the tile's Fourier features and each layer's
-// activations stay in shared memory, the accumulator in tensor memory, and
-// only the weights stream in (from L2: 1.7 MB for four members), as 32 KiB
+// activations stay in shared memory, the accumulators in tensor memory, and
+// only the weights stream in (from L2: 1.7 MB for four members), as 16 KiB
 // K-chunks copied by the bulk-copy engine (cp.async.bulk) into a 4-stage ring
 // kept three chunks ahead of the MMAs.
-// One thread issues the tcgen05 MMAs; all twelve warps run the epilogue (bias,
-// GELU, BF16 into the next layer's operand tile, or the head's dot product).
-// The arithmetic is the layered path's: same MMA sequence, the same epilogue
-// expressions and the head's and ensemble's summation orders, so the outputs
-// are the same numbers without the per-layer round trips through HBM.
+//
+// Two members are in flight at a time, on two "streams" with their own
+// 256-column TMEM accumulator and 128 x 256 activation tile: while the eight
+// epilogue warps apply bias and GELU to one member's layer (the expensive
+// part: an erf per element), the control warp issues the other member's MMAs
+// and weight copies.  The streams hand over through mbarriers: acc_full[s]
+// (the layer's MMAs are done), act_ready[s] (its epilogue has read the
+// accumulator and written the next operand), x0_ready (the tile's features).
+// The arithmetic is the layered path's: the same MMAs in the same K order,
+// the same epilogue expressions and the head's and ensemble's summation
+// orders, so the outputs are the same numbers without the per-layer round
+// trips through HBM.
 
-constexpr int kChunkBytes = kWidth * umma::kBK * 2;                    // one 256 x 64 BF16 weight chunk
-constexpr int kChunksPerMember = 1 + (kDepth - 1) * (kWidth / umma::kBK);  // 13
+constexpr int kWChunkK = 32;                                          // K per weight chunk
+constexpr int kChunkBytes = kWidth * kWChunkK * 2;                    // 256 rows x 32 BF16 = 16 KiB
+constexpr int kChunksPerMember = (kFeat + (kDepth - 1) * kWidth) / kWChunkK;   // 2 + 3 * 8 = 26
 constexpr int kInferStages = 4;
-constexpr int kInferThreads = 384;   // 12 warps: three per TMEM lane quarter
-constexpr int kTileRows = umma::kBM;                                    // 128
-constexpr int kActChunk = kTileRows * umma::kBK * 2;                   // 16 KiB
-constexpr int kMemberConsts = kDepth * kWidth + kWidth + 2;             // biases, w5, b5, pad
-constexpr int kGStride = 33;                                            // head partials per row (32 + pad)
-constexpr int kOffInferAct = kInferStages * kChunkBytes;
-constexpr int kOffInferX0 = kOffInferAct + (kWidth / umma::kBK) * kActChunk;
-constexpr int kOffInferC = kOffInferX0 + kActChunk;
-constexpr int kOffInferY = kOffInferC + ((kMemberConsts * 4 + 15) / 16) * 16;
-constexpr int kInferSmem = kOffInferY + kMaxMembers * kTileRows * 4;
-// the head's partial sums live in the activation tile, which the last
-// layer's MMAs have finished reading when the head writes them
-constexpr int kOffInferG = kOffInferAct;
-static_assert(kTileRows * kGStride * 4 <= (kWidth / umma::kBK) * kActChunk, "head partials fit the tile");
-static_assert(kInferSmem + 256 <= 227 * 1024, "fused inference shared memory");
+constexpr int kEpiWarps = 8;                                          // two per TMEM lane quarter
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kInferThreads = kEpiThreads + 32;                       // + the control warp
+constexpr int kTileRows = umma::kBM;                                  // 128
+constexpr int kActChunk = kTileRows * umma::kBK * 2;                 // 128 rows x 64 BF16 = 16 KiB
+constexpr int kActBytes = (kWidth / umma::kBK) * kActChunk;          // 64 KiB
+constexpr int kMemberConsts = kDepth * kWidth + kWidth + 2;           // biases, w5, b5, pad
+constexpr int kConstBytes = ((kMemberConsts * 4 + 15) / 16) * 16;
+constexpr int kGStride = 33;                                          // head partials per row (32 + pad)
+constexpr int kInferMaxMembers = 8;
+constexpr int kOffInferAct = kInferStages * kChunkBytes;             // two activation tiles
+constexpr int kOffInferX0 = kOffInferAct + 2 * kActBytes;
+constexpr int kOffInferC = kOffInferX0 + kActChunk;                  // two members' constants
+constexpr int kOffInferY = kOffInferC + 2 * kConstBytes;
+constexpr int kInferSmem = kOffInferY + kInferMaxMembers * kTileRows * 4;
+// the head's partial sums live in the stream's activation tile, which the
+// last layer's MMAs have finished reading when the head writes them
+static_assert(kTileRows * kGStride * 4 <= kActBytes, "head partials fit the activation tile");
+static_assert(kInferSmem + 512 <= 227 * 1024, "fused inference shared memory");
+
+// byte offset of element (r, k) of a rows x 32 K-major weight chunk in the
+// canonical no-swizzle layout (8-row groups 512 bytes apart)
+__host__ __device__ constexpr uint32_t wchunk_off(int r, int k)
+{
+    return (uint32_t)(((r >> 3) * (kWChunkK / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// The work of one tile as jobs (stream s, member e, layer l), in the order
+// both the control warp and the epilogue warps take them: members in pairs
+// (2p on stream 0, 2p + 1 on stream 1), layer by layer, alternating streams;
+// an odd last member alone on stream 0.
+__host__ __device__ inline void job_of(int j, int E, int &s, int &e, int &l)
+{
+    const int pairs = E / 2;
+    if (j < pairs * 2 * kDepth) {
+        const int p = j / (2 * kDepth), r = j % (2 * kDepth);
+        l = r / 2;
+        s = r % 2;
+        e = 2 * p + s;
+        return;
+    }
+    s = 0;
+    e = E - 1;
+    l = j - pairs * 2 * kDepth;
+}
+
+__host__ __device__ constexpr int job_chunks(int l) { return in_dim(l) / kWChunkK; }
+
+// Weight chunk c of the image (the control warp's consumption order):
+// member e, layer l, K-chunk kq
+__host__ __device__ inline void chunk_of(int c, int E, int &e, int &l, int &kq)
+{
+    int j = 0;
+    int s = 0;
+    for (;; j++) {
+        job_of(j, E, s, e, l);
+        const int n = job_chunks(l);
+        if (c < n) {
+            kq = c;
+            return;
+        }
+        c -= n;
+    }
+}
 
 struct WeightPtrs {
     const bf16 *w[kDepth];
 };
 
-// The weight image: for every member its 13 K-chunks (layer 0: one, layers
-// 1..3: four each) of W_l [256][K], each in the canonical no-swizzle K-major
-// layout of a 256 x 64 tile, in the order the fused kernel consumes them.
+// The weight image: for every member its 26 K-chunks of W_l [256][K], each in
+// the canonical no-swizzle K-major layout of a 256 x 32 tile, in the order the
+// fused kernel consumes them.
 __global__ void weight_image_kernel(WeightPtrs W, int E, uint8_t *__restrict__ img)
 {
     constexpr int kPieces = kChunkBytes / 16;   // 16-byte pieces (8 BF16 along K) per chunk
     const long long total = (long long)E * kChunksPerMember * kPieces;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
-        const long long c = t / kPieces;
-        const int p = (int)(t - c * kPieces);
-        const int e = (int)(c / kChunksPerMember);
-        const int q = (int)(c - (long long)e * kChunksPerMember);
-        const int l = q == 0 ? 0 : 1 + (q - 1) / (kWidth / umma::kBK);
-        const int kq = q == 0 ? 0 : (q - 1) % (kWidth / umma::kBK);
+        const int c = (int)(t / kPieces);
+        const int p = (int)(t - (long long)c * kPieces);
+        int e, l, kq;
+        chunk_of(c, E, e, l, kq);
         const int K = in_dim(l);
-        const int r = p >> 3, kc = p & 7;
-        const bf16 *src = W.w[l] + (long long)e * kWidth * K + (long long)r * K + kq * umma::kBK + kc * 8;
-        *reinterpret_cast<uint4 *>(img + c * kChunkBytes + umma::tile_off(r, kc * 8)) =
+        const int r = p >> 2, kc = p & 3;
+        const bf16 *src = W.w[l] + (long long)e * kWidth * K + (long long)r * K + kq * kWChunkK + kc * 8;
+        *reinterpret_cast<uint4 *>(img + (long long)c * kChunkBytes + wchunk_off(r, kc * 8)) =
             *reinterpret_cast<const uint4 *>(src);
     }
 }
@@ -675,6 +730,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_u32(bar)) : "memory");
+}
+
 // bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
 // from global to this CTA's shared memory, completing on `bar`
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
@@ -683,6 +743,40 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                      umma::smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(umma::smem_u32(bar))
                  : "memory");
+}
+
+// bounded wait that also gives up once another thread has aborted the CTA;
+// a thread whose own wait runs out raises the abort flag
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort)
+{
+    const uint32_t addr = umma::smem_u32(bar);
+    for (unsigned it = 0; it < umma::kWaitLimit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done)
+            return true;
+        if ((it & 255u) == 255u && *abort)
+            return false;
+    }
+    *abort = 1;
+    return false;
+}
+
+// barrier over the eight epilogue warps (named barrier 1) that also ANDs a
+// predicate across them: every epilogue thread takes the same branch after it
+__device__ __forceinline__ bool epi_sync_and(bool ok)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)ok), "r"(kEpiThreads)
+        : "memory");
+    return r != 0;
 }
 
 struct InferArgs {
@@ -711,139 +805,179 @@ __device__ __forceinline__ float member_const(const float *P, int i)
 __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t full[kInferStages], empty[kInferStages], accb;
+    __shared__ uint64_t full[kInferStages], empty[kInferStages], acc_full[2], act_ready[2], x0_ready;
     __shared__ uint32_t tslot;
+    __shared__ int s_abort;
     uint8_t *Ws = smem;
-    uint8_t *Act = smem + kOffInferAct;
     uint8_t *X0s = smem + kOffInferX0;
-    float *cst = reinterpret_cast<float *>(smem + kOffInferC);
-    float *gs = reinterpret_cast<float *>(smem + kOffInferG);
     float *ys = reinterpret_cast<float *>(smem + kOffInferY);
+    volatile int *abort = &s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long long tiles = (a.n + kTileRows - 1) / kTileRows;
     const long long my_tiles = tiles > (long long)blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-    const long long per_tile = (long long)a.E * kChunksPerMember;
-    const long long total = my_tiles * per_tile;
+    const int jobs = kDepth * a.E;
 
     if (tid == 0) {
         for (int s = 0; s < kInferStages; s++) {
             umma::mbar_init(&full[s], 1);
             umma::mbar_init(&empty[s], 1);
         }
-        umma::mbar_init(&accb, 1);
+        for (int s = 0; s < 2; s++) {
+            umma::mbar_init(&acc_full[s], 1);
+            umma::mbar_init(&act_ready[s], kEpiThreads);
+        }
+        umma::mbar_init(&x0_ready, kEpiThreads);
+        s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0)
-        umma::tmem_alloc(&tslot, kWidth);
+        umma::tmem_alloc(&tslot, 2 * kWidth);   // one accumulator per stream
     umma::tc_fence_before();
     __syncthreads();
     umma::tc_fence_after();
     const uint32_t tmem = tslot;
-    constexpr uint32_t idesc = umma::idesc_bf16_f32(kWidth);
 
-    bool ok = true;
-    long long q_issue = 0, q_use = 0;   // thread 0: next weight chunk to load / to consume
-    uint32_t acc_phase = 0;
-    // thread 0: load weight chunk q into stage q % kInferStages once the MMAs
-    // that read that stage's previous chunk are done
-    auto issue = [&](long long q) -> bool {
-        const int s = (int)(q % kInferStages);
-        if (q >= kInferStages && !umma::mbar_wait(&empty[s], (uint32_t)((q / kInferStages - 1) & 1)))
-            return false;
-        mbar_expect_tx(&full[s], kChunkBytes);
-        bulk_g2s(Ws + s * kChunkBytes, a.wimg + (q % per_tile) * kChunkBytes, kChunkBytes, &full[s]);
-        return true;
-    };
-    if (tid == 0)
-        for (; q_issue < total && q_issue < kInferStages - 1; q_issue++)
-            ok = issue(q_issue) && ok;
-
-    const int rl = 32 * (warp & 3) + lane;     // this thread's row of the tile (TMEM lane)
-    // its accumulator columns: warps 0-3 take 0..95, 4-7 96..175, 8-11 176..255
-    const int cb = warp < 4 ? 0 : (warp < 8 ? 96 : 176);
-    const int ce = warp < 4 ? 96 : (warp < 8 ? 176 : kWidth);
-    for (long long ti = 0; ti < my_tiles && ok; ti++) {
-        const long long row0 = (blockIdx.x + ti * gridDim.x) * kTileRows;
-        // Fourier features of the tile (features_kernel's expressions), BF16
-        // into the layer-0 operand tile; rows past n are zeros
-        if (tid < 2 * kTileRows) {
-            const int r = tid >> 1, h = tid & 1;
-            const long long i = row0 + r;
-            float sv[16], cv[16];
-#pragma unroll
-            for (int jj = 0; jj < 16; jj++) {
-                sv[jj] = 0.0f;
-                cv[jj] = 0.0f;
-            }
-            if (i < a.n) {
-                const float *x = a.x7 + 7 * i;
-#pragma unroll
-                for (int jj = 0; jj < 16; jj++) {
-                    const int j = 16 * h + jj;
-                    float p = 0.0f;
-#pragma unroll
-                    for (int q = 0; q < kIn; q++)
-                        p += a.Bf[j * kIn + q] * x[q];
-                    sincospif(2.0f * p, &sv[jj], &cv[jj]);
-                }
-            }
-#pragma unroll
-            for (int part = 0; part < 4; part++) {   // features 16h..16h+15 (sin) and 32+16h.. (cos)
-                const float *src = part < 2 ? sv + 8 * part : cv + 8 * (part - 2);
-                const int f0 = (part < 2 ? 0 : kFeat / 2) + 16 * h + 8 * (part & 1);
-                __align__(16) bf16 t[8];
-#pragma unroll
-                for (int q = 0; q < 8; q++)
-                    t[q] = __float2bfloat16_rn(src[q]);
-                *reinterpret_cast<uint4 *>(X0s + umma::tile_off(r, f0)) = *reinterpret_cast<const uint4 *>(t);
-            }
-        }
-        umma::fence_async_smem();
-        for (int e = 0; e < a.E && ok; e++) {
-            __syncthreads();   // the previous member's head is done with cst
-            for (int i = tid; i < kMemberConsts; i += kInferThreads)
-                cst[i] = member_const(a.params + (long long)e * kParams, i);
-            for (int l = 0; l < kDepth; l++) {
-                const int nk = in_dim(l) / umma::kBK;
-                // the operand tile and the constants are written; the previous
-                // layer's accumulator reads are done
-                umma::tc_fence_before();
-                ok = __syncthreads_and(ok);
-                if (!ok)
-                    break;
-                if (tid == 0) {
+    if (warp == kEpiWarps) {
+        // ---- control warp: lane 0 issues the weight copies and the MMAs
+        if (lane == 0) {
+            constexpr uint32_t idesc = umma::idesc_bf16_f32(kWidth);
+            const long long per_tile = (long long)a.E * kChunksPerMember;
+            const long long total = my_tiles * per_tile;
+            long long q_issue = 0, q_use = 0;
+            uint32_t kjob[2] = {0u, 0u};
+            bool ok = true;
+            // load weight chunk q into stage q % kInferStages once the MMAs that
+            // read that stage's previous chunk are done
+            auto issue = [&](long long q) -> bool {
+                const int st = (int)(q % kInferStages);
+                if (q >= kInferStages &&
+                    !wait_or_abort(&empty[st], (uint32_t)((q / kInferStages - 1) & 1), abort))
+                    return false;
+                mbar_expect_tx(&full[st], kChunkBytes);
+                bulk_g2s(Ws + st * kChunkBytes, a.wimg + (q % per_tile) * kChunkBytes, kChunkBytes, &full[st]);
+                return true;
+            };
+            for (; q_issue < total && q_issue < kInferStages - 1 && ok; q_issue++)
+                ok = issue(q_issue);
+            for (long long ti = 0; ti < my_tiles && ok; ti++) {
+                for (int j = 0; j < jobs && ok; j++) {
+                    int s, e, l;
+                    job_of(j, a.E, s, e, l);
+                    // the operand: the tile's features (layer 0) or the stream's
+                    // previous epilogue, which also freed its accumulator
+                    if (j == 0)
+                        ok = wait_or_abort(&x0_ready, (uint32_t)(ti & 1), abort);
+                    if (ok && kjob[s] > 0)
+                        ok = wait_or_abort(&act_ready[s], (kjob[s] - 1u) & 1u, abort);
+                    if (!ok)
+                        break;
                     umma::tc_fence_after();
-                    for (int kc = 0; kc < nk && ok; kc++, q_use++) {
-                        const int s = (int)(q_use % kInferStages);
-                        if (!umma::mbar_wait(&full[s], (uint32_t)((q_use / kInferStages) & 1))) {
+                    const uint8_t *A = l == 0 ? X0s : smem + kOffInferAct + s * kActBytes;
+                    const int nk = job_chunks(l);
+                    for (int kc = 0; kc < nk; kc++, q_use++) {
+                        const int st = (int)(q_use % kInferStages);
+                        if (!wait_or_abort(&full[st], (uint32_t)((q_use / kInferStages) & 1), abort)) {
                             ok = false;
                             break;
                         }
-                        const uint32_t a0 = umma::smem_u32(l == 0 ? X0s : Act + kc * kActChunk);
-                        const uint32_t b0 = umma::smem_u32(Ws + s * kChunkBytes);
 #pragma unroll
-                        for (int kk = 0; kk < umma::kBK / 16; kk++)
-                            umma::mma_bf16(tmem, umma::smem_desc(a0 + kk * 256, 128, 1024),
-                                           umma::smem_desc(b0 + kk * 256, 128, 1024), idesc,
-                                           (kc > 0 || kk > 0) ? 1u : 0u);
-                        umma::mma_commit(&empty[s]);
+                        for (int kk = 0; kk < kWChunkK / 16; kk++) {
+                            const int k0 = kc * kWChunkK + kk * 16;
+                            const uint32_t a0 = umma::smem_u32(A + (k0 / umma::kBK) * kActChunk) +
+                                                (uint32_t)((k0 % umma::kBK) / 16) * 256;
+                            const uint32_t b0 = umma::smem_u32(Ws + st * kChunkBytes) + (uint32_t)kk * 256;
+                            umma::mma_bf16(tmem + (uint32_t)(s * kWidth), umma::smem_desc(a0, 128, 1024),
+                                           umma::smem_desc(b0, 128, 512), idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+                        }
+                        umma::mma_commit(&empty[st]);
                         if (q_issue < total) {
-                            ok = issue(q_issue) && ok;
+                            if (!issue(q_issue)) {
+                                ok = false;
+                                q_use++;
+                                break;
+                            }
                             q_issue++;
                         }
                     }
-                    umma::mma_commit(&accb);
+                    umma::mma_commit(&acc_full[s]);
+                    kjob[s]++;
                 }
-                // the layer's accumulator (a failed issue leaves it
-                // uncommitted: the bounded wait then fails too)
-                ok = umma::mbar_wait(&accb, acc_phase) && ok;
-                acc_phase ^= 1u;
+            }
+            // copies still in flight complete before the CTA's shared memory
+            // goes away (bounded: a failed copy does not hold the exit)
+            for (long long q = q_use; q < q_issue; q++)
+                wait_or_abort(&full[q % kInferStages], (uint32_t)((q / kInferStages) & 1), abort);
+            if (!ok)
+                *abort = 1;
+        }
+    } else {
+        // ---- epilogue warps: features, bias + GELU per layer, head, ensemble
+        const int rl = 32 * (warp & 3) + lane;          // this thread's row of the tile (TMEM lane)
+        const int cb = (warp >> 2) * (kWidth / 2);      // its 128 accumulator columns
+        uint32_t ejob[2] = {0u, 0u};
+        bool ok = true;
+        for (long long ti = 0; ti < my_tiles && ok; ti++) {
+            const long long row0 = (blockIdx.x + ti * gridDim.x) * kTileRows;
+            {
+                // Fourier features of the tile (features_kernel's expressions),
+                // BF16 into the layer-0 operand tile; rows past n are zeros
+                const int r = tid >> 1, h = tid & 1;
+                const long long i = row0 + r;
+                float sv[16], cv[16];
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++) {
+                    sv[jj] = 0.0f;
+                    cv[jj] = 0.0f;
+                }
+                if (i < a.n) {
+                    const float *x = a.x7 + 7 * i;
+#pragma unroll
+                    for (int jj = 0; jj < 16; jj++) {
+                        const int j = 16 * h + jj;
+                        float p = 0.0f;
+#pragma unroll
+                        for (int q = 0; q < kIn; q++)
+                            p += a.Bf[j * kIn + q] * x[q];
+                        sincospif(2.0f * p, &sv[jj], &cv[jj]);
+                    }
+                }
+#pragma unroll
+                for (int part = 0; part < 4; part++) {   // features 16h.. (sin) and 32+16h.. (cos)
+                    const float *src = part < 2 ? sv + 8 * part : cv + 8 * (part - 2);
+                    const int f0 = (part < 2 ? 0 : kFeat / 2) + 16 * h + 8 * (part & 1);
+                    __align__(16) bf16 t[8];
+#pragma unroll
+                    for (int q = 0; q < 8; q++)
+                        t[q] = __float2bfloat16_rn(src[q]);
+                    *reinterpret_cast<uint4 *>(X0s + umma::tile_off(r, f0)) = *reinterpret_cast<const uint4 *>(t);
+                }
+            }
+            umma::fence_async_smem();
+            mbar_arrive(&x0_ready);
+            for (int j = 0; j < jobs; j++) {
+                int s, e, l;
+                job_of(j, a.E, s, e, l);
+                float *cst = reinterpret_cast<float *>(smem + kOffInferC + s * kConstBytes);
+                uint8_t *Act = smem + kOffInferAct + s * kActBytes;
+                if (l == 0) {
+                    // this member's constants (the stream's previous member is done with them)
+                    for (int i = tid; i < kMemberConsts; i += kEpiThreads)
+                        cst[i] = member_const(a.params + (long long)e * kParams, i);
+                }
+                ok = wait_or_abort(&acc_full[s], ejob[s] & 1u, abort) && ok;
+                ejob[s]++;
+                ok = epi_sync_and(ok);   // also publishes the constants
+                if (!ok)
+                    break;
                 umma::tc_fence_after();
                 const float *bias = cst + l * kWidth;
                 const float *w5 = cst + kDepth * kWidth;
-                for (int c0 = cb; c0 < ce; c0 += 16) {
+                float *gs = reinterpret_cast<float *>(Act);
+                for (int c0 = cb; c0 < cb + kWidth / 2; c0 += 16) {
                     float v[16];
-                    umma::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c0, v);
+                    umma::tmem_ld16(tmem + (uint32_t)(s * kWidth) + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                        (uint32_t)c0,
+                                    v);
 #pragma unroll
                     for (int q = 0; q < 16; q++)
                         v[q] = gelu(v[q] + bias[c0 + q]);
@@ -870,65 +1004,61 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
                         }
                     }
                 }
+                umma::tc_fence_before();
                 umma::fence_async_smem();
+                if (l == kDepth - 1) {
+                    epi_sync_and(true);
+                    if (tid < kTileRows) {
+                        // head_kernel's shuffle tree over the 32 partial sums (lane 0's order)
+                        float g[32];
+#pragma unroll
+                        for (int jj = 0; jj < 32; jj++)
+                            g[jj] = gs[tid * kGStride + jj];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                            for (int jj = 0; jj < o; jj++)
+                                g[jj] = g[jj] + g[jj + o];
+                        ys[e * kTileRows + tid] = g[0] + cst[kDepth * kWidth + kWidth];
+                    }
+                    epi_sync_and(true);
+                }
+                mbar_arrive(&act_ready[s]);
             }
-            ok = __syncthreads_and(ok);   // uniform again: every thread takes the same branch
             if (!ok)
                 break;
-            if (tid < kTileRows) {
-                // head_kernel's shuffle tree over the 32 partial sums (lane 0's order)
-                float g[32];
+            if (tid < kTileRows && row0 + tid < a.n) {
+                // ensemble_kernel's statistics (this thread's own row of ys)
+                const long long i = row0 + tid;
+                float av[kInferMaxMembers];
+                float sum = 0.0f;
 #pragma unroll
-                for (int j = 0; j < 32; j++)
-                    g[j] = gs[tid * kGStride + j];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-                    for (int j = 0; j < o; j++)
-                        g[j] = g[j] + g[j + o];
-                ys[e * kTileRows + tid] = g[0] + cst[kDepth * kWidth + kWidth];
-            }
-        }
-        ok = __syncthreads_and(ok);
-        if (!ok)
-            break;
-        if (tid < kTileRows && row0 + tid < a.n) {
-            // ensemble_kernel's statistics
-            const long long i = row0 + tid;
-            float av[kMaxMembers];
-            float sum = 0.0f;
-#pragma unroll
-            for (int e = 0; e < kMaxMembers; e++) {
-                if (e < a.E) {
-                    const float la = a.mu + a.sd * ys[e * kTileRows + tid];
-                    if (a.members)
-                        a.members[e * a.ldm + i] = la;
-                    av[e] = expf(la);
-                    sum += av[e];
+                for (int e = 0; e < kInferMaxMembers; e++) {
+                    if (e < a.E) {
+                        const float la = a.mu + a.sd * ys[e * kTileRows + tid];
+                        if (a.members)
+                            a.members[e * a.ldm + i] = la;
+                        av[e] = expf(la);
+                        sum += av[e];
+                    }
                 }
-            }
-            const float m = sum / a.E;
-            float var = 0.0f;
+                const float m = sum / a.E;
+                float var = 0.0f;
 #pragma unroll
-            for (int e = 0; e < kMaxMembers; e++)
-                if (e < a.E)
-                    var += (av[e] - m) * (av[e] - m);
-            a.mean[i] = m;
-            a.spread[i] = sqrtf(var / a.E) / m;
+                for (int e = 0; e < kInferMaxMembers; e++)
+                    if (e < a.E)
+                        var += (av[e] - m) * (av[e] - m);
+                a.mean[i] = m;
+                a.spread[i] = sqrtf(var / a.E) / m;
+            }
         }
-    }
-    if (tid == 0) {
-        // weight chunks still in flight complete before the CTA's shared
-        // memory goes away (bounded: a failed copy does not hold the exit)
-        for (long long q = q_use; q < q_issue; q++)
-            umma::mbar_wait(&full[q % kInferStages], (uint32_t)((q / kInferStages) & 1));
-        if (!ok)
-            atomicOr(a.err, 1);
     }
     umma::tc_fence_before();
     __syncthreads();
+    if (tid == 0 && s_abort)
+        atomicOr(a.err, 1);
     if (warp == 0)
-        umma::tmem_dealloc(tmem, kWidth);
+        umma::tmem_dealloc(tmem, 2 * kWidth);
 }
 
 std::once_flag g_infer_once[64];
@@ -1540,7 +1670,7 @@ int anacor_surrogate_predict_device(anacor_surrogate *s, const float *d_x7, int6
     if (n == 0)
         return report_status(kOk, "");
     cudaStream_t st = stream ? (cudaStream_t)stream : s->st;
-    if (s->fused) {
+    if (s->fused && s->E <= kInferMaxMembers) {
         // one launch over all n rows: no activation workspace
         int dev = 0, sms = 0;
         cudaError_t e;

@@ -202,6 +202,23 @@ def test_fused_inference_matches_layered(small, trained_small):
     assert np.allclose(s1_, s0, rtol=1e-4, atol=1e-8)
 
 
+@pytest.mark.parametrize("members", [1, 3])
+def test_fused_inference_matches_layered_odd_members(members):
+    """The fused kernel runs members two at a time; an odd last member runs
+    alone.  Untrained (seeded) weights, rows not a multiple of the tile."""
+    rng = np.random.default_rng(members)
+    x7 = rng.uniform(-1.0, 1.0, size=(3001, 7)).astype(np.float32)
+    model = surrogate.Surrogate(members=members, seed=11, fourier_scale=0.5)
+    try:
+        model.set_inference(False)
+        m0, s0, e0 = model.predict(x7, members=True)
+        model.set_inference(True)
+        m1, s1, e1 = model.predict(x7, members=True)
+    finally:
+        model.close()
+    assert np.array_equal(e1, e0) and np.array_equal(m1, m0) and np.array_equal(s1, s0)
+
+
 def test_audited_absorption_small(small, trained_small):
     model, _ = trained_small
     rng = np.random.default_rng(99)

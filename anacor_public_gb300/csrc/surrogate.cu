@@ -619,7 +619,7 @@ __global__ void audit_kernel(const float *__restrict__ spread, long long n, uint
 // kept three chunks ahead of the MMAs.
 //
 // Two members are in flight at a time, on two "streams" with their own
-// 256-column TMEM accumulator and 128 x 256 activation tile: while the eight
+// 256-column TMEM accumulator and 128 x 256 activation tile: while the twelve
 // epilogue warps apply bias and GELU to one member's layer (the expensive
 // part: an erf per element), the control warp issues the other member's MMAs
 // and weight copies.  The streams hand over through mbarriers: acc_full[s]
@@ -634,7 +634,7 @@ constexpr int kWChunkK = 32;                                          // K per w
 constexpr int kChunkBytes = kWidth * kWChunkK * 2;                    // 256 rows x 32 BF16 = 16 KiB
 constexpr int kChunksPerMember = (kFeat + (kDepth - 1) * kWidth) / kWChunkK;   // 2 + 3 * 8 = 26
 constexpr int kInferStages = 4;
-constexpr int kEpiWarps = 8;                                          // two per TMEM lane quarter
+constexpr int kEpiWarps = 12;                                         // three per TMEM lane quarter
 constexpr int kEpiThreads = 32 * kEpiWarps;
 constexpr int kInferThreads = kEpiThreads + 32;                       // + the control warp
 constexpr int kTileRows = umma::kBM;                                  // 128
@@ -766,7 +766,7 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, vo
     return false;
 }
 
-// barrier over the eight epilogue warps (named barrier 1) that also ANDs a
+// barrier over the epilogue warps (named barrier 1) that also ANDs a
 // predicate across them: every epilogue thread takes the same branch after it
 __device__ __forceinline__ bool epi_sync_and(bool ok)
 {
@@ -913,12 +913,14 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
     } else {
         // ---- epilogue warps: features, bias + GELU per layer, head, ensemble
         const int rl = 32 * (warp & 3) + lane;          // this thread's row of the tile (TMEM lane)
-        const int cb = (warp >> 2) * (kWidth / 2);      // its 128 accumulator columns
+        // its accumulator columns: warps 0-3 take 0..95, 4-7 96..175, 8-11 176..255
+        const int cb = warp < 4 ? 0 : (warp < 8 ? 96 : 176);
+        const int ce = warp < 4 ? 96 : (warp < 8 ? 176 : kWidth);
         uint32_t ejob[2] = {0u, 0u};
         bool ok = true;
         for (long long ti = 0; ti < my_tiles && ok; ti++) {
             const long long row0 = (blockIdx.x + ti * gridDim.x) * kTileRows;
-            {
+            if (tid < 2 * kTileRows) {
                 // Fourier features of the tile (features_kernel's expressions),
                 // BF16 into the layer-0 operand tile; rows past n are zeros
                 const int r = tid >> 1, h = tid & 1;
@@ -973,7 +975,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
                 const float *bias = cst + l * kWidth;
                 const float *w5 = cst + kDepth * kWidth;
                 float *gs = reinterpret_cast<float *>(Act);
-                for (int c0 = cb; c0 < cb + kWidth / 2; c0 += 16) {
+                for (int c0 = cb; c0 < ce; c0 += 16) {
                     float v[16];
                     umma::tmem_ld16(tmem + (uint32_t)(s * kWidth) + ((uint32_t)(32 * (warp & 3)) << 16) +
                                         (uint32_t)c0,

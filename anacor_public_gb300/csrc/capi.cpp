@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -739,23 +740,32 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
              const double *xray, const double *axis, const double *F, const ReflTable *tables, int threads,
              double *out, int ib_cls = 0)
 {
+    // the tables go through this thread's pinned staging (no pinned
+    // allocation per call); the plan lives for this call only
+    ReflTable *staged = n_refl > 0 ? thread_staging(n_refl) : nullptr;
+    // The reflections' host set-up (FP64 rotation, angles, face rules) does
+    // not depend on the device: it runs on a second host thread while this
+    // one uploads the volume and voxels and builds the march's fields.
+    std::future<int> setup;
+    if (staged && !tables)
+        setup = std::async(std::launch::async, [=] {
+            return setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads);
+        });
     anacor_plan p;
     int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
     if (!st) {
-        // the tables go through this thread's pinned staging (no pinned
-        // allocation per call); the plan lives for this call only
-        p.h_refl = thread_staging(n_refl);
-        p.h_refl_borrowed = p.h_refl != nullptr;
-        if (!p.h_refl_borrowed)
-            p.h_refl = nullptr;
+        p.h_refl = staged;
+        p.h_refl_borrowed = staged != nullptr;
         st = plan_reserve_refl(&p, n_refl);
     }
     if (!st && !ib_cls)
         st = plan_default_config(&p);
+    const int setup_st = setup.valid() ? setup.get() : kOk;   // joined on every path
     if (!st) {
         if (tables)
             std::memcpy(p.h_refl, tables, (size_t)n_refl * sizeof(ReflTable));
-        else if (n_refl > 0 && (st = setup_reflections(axis, omega, F, xray, s1, n_refl, p.h_refl, threads)))
+        else if (n_refl > 0 &&
+                 (st = staged ? setup_st : setup_reflections(axis, omega, F, xray, s1, n_refl, p.h_refl, threads)))
             fail(st, status_text(st));
     }
     if (!st)

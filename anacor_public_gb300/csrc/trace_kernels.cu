@@ -93,20 +93,29 @@ struct Vol {
 // a 32-byte sector holds a 2x4x4 (z, y, x) box.  A ray that steps by one voxel
 // along any axis mostly stays in the sector its previous load brought into L1
 // (in the linear layout only steps along x do).
-__device__ __forceinline__ int brick_term(int u, int bs, int sh)
+//
+// Axis coordinate u = 4 U + w contributes U * BS + w * IS (BS the axis's
+// brick stride, IS its stride inside a brick), which equals
+// (u & ~3) * K + u * IS with K = BS / 4 - IS: a mask and two multiply-adds.
+__device__ __forceinline__ int brick_term(int u, int k, int is)
 {
-    return (u >> 2) * bs + ((u & 3) << sh);
+    return (u & ~3) * k + u * is;
 }
 
-__device__ __forceinline__ int brick_offset(int z, int y, int x, int bsy, int bsz)
+// K and IS of axis a (0 z, 1 y, 2 x)
+__device__ __forceinline__ int brick_k(int a, const Vol &v)
 {
-    return brick_term(z, bsz, 4) + brick_term(y, bsy, 2) + brick_term(x, 64, 0);
+    return a == 0 ? v.bsz / 4 - 16 : (a == 1 ? v.bsy / 4 - 4 : 64 / 4 - 1);
 }
 
-// brick stride and in-brick shift of axis k (0 z, 1 y, 2 x)
-__device__ __forceinline__ int brick_stride(int k, const Vol &v)
+__device__ __forceinline__ int brick_is(int a)
 {
-    return k == 0 ? v.bsz : (k == 1 ? v.bsy : 64);
+    return 16 >> (2 * a);
+}
+
+__device__ __forceinline__ int brick_offset(int z, int y, int x, const Vol &v)
+{
+    return brick_term(z, brick_k(0, v), 16) + brick_term(y, brick_k(1, v), 4) + brick_term(x, brick_k(2, v), 1);
 }
 
 __device__ __forceinline__ int pick3(int k, int z, int y, int x)
@@ -370,7 +379,7 @@ __device__ __noinline__ uint32_t exact_byte(const FaceRule &G, int cz, int cy, i
     pz = s == 0 ? cz + inc * ds : exact_axis(cz, inc, G.q[0], G.use_round, v.dz);
     py = s == 1 ? cy + inc * ds : exact_axis(cy, inc, G.q[1], G.use_round, v.dy);
     px = s == 2 ? cx + inc * ds : exact_axis(cx, inc, G.q[2], G.use_round, v.dx);
-    return (uint32_t)__ldg(bytes + (brick ? brick_offset(pz, py, px, v.bsy, v.bsz) : (pz * v.dy + py) * v.dx + px));
+    return (uint32_t)__ldg(bytes + (brick ? brick_offset(pz, py, px, v) : (pz * v.dy + py) * v.dx + px));
 }
 
 __device__ __forceinline__ uint32_t exact_label(const FaceRule &G, int cz, int cy, int cx, int inc, const Vol &v)
@@ -419,8 +428,8 @@ struct FieldChain {
     uint32_t Ma, Mb, rq;
     int dS, Sa, Sb;           // linear: strides of the step axis (signed) and the two others
     int cs, ds;               // bricked: start coordinate and direction on the step axis
-    int bs_s, bs_a, bs_b;     // bricked: brick strides of the step axis and the two others
-    int sh_s, sh_a, sh_b;     // bricked: their in-brick shifts
+    int k_s, k_a, k_b;        // bricked: brick_term's K of the step axis and the two others
+    int is_s, is_a, is_b;     // bricked: their in-brick strides
     int i, lim, last, prev, nseg;
     bool on;
 };
@@ -448,12 +457,12 @@ __device__ __forceinline__ void chain_init(FieldChain &c, const FaceRule &R, con
         c.cs = g.cs;
         c.ds = g.ds;
         const int s = R.count_axis;
-        c.bs_s = brick_stride(s, v);
-        c.bs_a = brick_stride(g.ia, v);
-        c.bs_b = brick_stride(g.ib, v);
-        c.sh_s = 4 - 2 * s;
-        c.sh_a = 4 - 2 * g.ia;
-        c.sh_b = 4 - 2 * g.ib;
+        c.k_s = brick_k(s, v);
+        c.k_a = brick_k(g.ia, v);
+        c.k_b = brick_k(g.ib, v);
+        c.is_s = brick_is(s);
+        c.is_a = brick_is(g.ia);
+        c.is_b = brick_is(g.ib);
     } else {
         c.pk = fld + base;
         c.off = g.off;
@@ -478,8 +487,8 @@ __device__ __forceinline__ uint32_t chain_load(const FieldChain &c, int cz, int 
     if (((uint32_t)ea + c.Ma < 2u * c.Ma) | ((uint32_t)eb + c.Mb < 2u * c.Mb))
         return exact_byte(*c.R, cz, cy, cx, c.i, v, c.fld, kBrick);
     if (kBrick)
-        return __ldg(c.fld + (brick_term(c.cs + c.i * c.ds, c.bs_s, c.sh_s) + brick_term((int)(ea >> 32), c.bs_a, c.sh_a) +
-                              brick_term((int)(eb >> 32), c.bs_b, c.sh_b)));
+        return __ldg(c.fld + (brick_term(c.cs + c.i * c.ds, c.k_s, c.is_s) + brick_term((int)(ea >> 32), c.k_a, c.is_a) +
+                              brick_term((int)(eb >> 32), c.k_b, c.is_b)));
     return __ldg(c.pk + (c.i * c.dS + (int)(ea >> 32) * c.Sa + (int)(eb >> 32) * c.Sb));
 }
 
@@ -716,7 +725,7 @@ __device__ __forceinline__ void leg_setup(const LegHead &h, const FaceRule *rule
             if (kField) {
                 // per lane, no warp synchronisation: the field march
                 const uint8_t *fld = v.field + R.octant * v.field_stride;
-                b0 = __ldg(fld + (kBrick ? brick_offset(cz, cy, cx, v.bsy, v.bsz) : base));
+                b0 = __ldg(fld + (kBrick ? brick_offset(cz, cy, cx, v) : base));
                 if ((b0 & 7u) == 0) {
                     stopped = true;
                 } else {

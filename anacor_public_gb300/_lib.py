@@ -44,7 +44,7 @@ EXPORTS = (
     "anacor_plan_create_sampled", "anacor_plan_n_voxels", "anacor_plan_voxels", "anacor_sample_voxels",
     "anacor_plan_run_bisection", "anacor_bisection", "anacor_gridding_prepare", "anacor_gridding_run",
     "anacor_distance_field", "anacor_batch_kernels", "anacor_octant_fields", "anacor_block_guard_check",
-    "anacor_surrogate_set_inference",
+    "anacor_surrogate_set_inference", "anacor_wait_guard_check",
 )
 
 _LIB = None
@@ -133,6 +133,8 @@ def load(path: str | None = None) -> ct.CDLL:
     L.anacor_leg_detail.restype = ct.c_int
     L.anacor_leg_detail.argtypes = [_i8p, _i64p, _i64p, ct.c_int64, _f64p, _f64p, _f64p, ct.c_int,
                                     _i32p, _i32p, _i32p, _i32p, _i32p, _f64p, _i32p]
+    L.anacor_wait_guard_check.restype = ct.c_int
+    L.anacor_wait_guard_check.argtypes = [ct.c_uint, ct.POINTER(ct.c_int32)]
     L.anacor_surrogate_set_inference.restype = ct.c_int
     L.anacor_surrogate_set_inference.argtypes = [ct.c_void_p, ct.c_int]
     L.anacor_block_guard_check.restype = ct.c_int

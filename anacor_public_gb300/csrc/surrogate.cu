@@ -1063,6 +1063,35 @@ __global__ void __launch_bounds__(kInferThreads, 1) infer_kernel(InferArgs a)
         umma::tmem_dealloc(tmem, 2 * kWidth);
 }
 
+// The error path of the tensor-core kernels' bounded waits, on its own: a CTA
+// allocates tensor memory as they do, waits for an mbarrier phase that
+// nothing completes (an arrival count of 2 with one arrival) with an
+// iteration limit, then records the error, releases the tensor memory and
+// returns.
+__global__ void wait_guard_kernel(unsigned limit, int *err)
+{
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar, 2);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (threadIdx.x < 32)
+        umma::tmem_alloc(&tslot, 32);
+    umma::tc_fence_before();
+    __syncthreads();
+    umma::tc_fence_after();
+    if (threadIdx.x == 0)
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_u32(&bar)) : "memory");
+    const bool ok = umma::mbar_wait(&bar, 0u, limit);
+    if (!__syncthreads_and(ok) && threadIdx.x == 0)
+        atomicOr(err, 1);
+    umma::tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32)
+        umma::tmem_dealloc(tslot, 32);
+}
+
 std::once_flag g_infer_once[64];
 cudaError_t g_infer_init_err[64];
 
@@ -1831,6 +1860,27 @@ int anacor_surrogate_load(anacor_surrogate *s, const char *path)
         s->n_data = 0;
         drop_graph(s);
     }
+    return report_status(kOk, "");
+}
+
+int anacor_wait_guard_check(unsigned iterations, int32_t *status)
+{
+    if (!status || iterations == 0 || iterations > (1u << 20))
+        return report_status(kErrArgs, "iterations must lie in [1, 2^20]");
+    int *d_err = nullptr;
+    cudaError_t e;
+    if ((e = dalloc(&d_err, 1)))
+        return cuda_fail(e);
+    int h = 0;
+    if (!(e = cudaMemset(d_err, 0, sizeof(int)))) {
+        wait_guard_kernel<<<1, 128>>>(iterations, d_err);
+        if (!(e = cudaGetLastError()) && !(e = cudaDeviceSynchronize()))
+            e = cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    }
+    dfree(d_err);
+    if (e)
+        return cuda_fail(e);
+    *status = h;
     return report_status(kOk, "");
 }
 

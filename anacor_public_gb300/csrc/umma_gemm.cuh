@@ -56,10 +56,10 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 }
 
 // bounded wait for the mbarrier phase `parity`; returns false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned limit = kWaitLimit)
 {
     const uint32_t a = smem_u32(bar);
-    for (unsigned it = 0; it < kWaitLimit; it++) {
+    for (unsigned it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -406,6 +406,11 @@ int anacor_surrogate_load(anacor_surrogate *s, const char *path);
  * A [batch][M][K], B [batch][N][K] rounded to BF16, FP32 accumulation, the K
  * range split into ksplit slices whose partial products are summed in order */
 int anacor_tc_gemm_check(const float *A, const float *B, int M, int N, int K, int batch, int ksplit, float *C);
+/* The error path of the tensor-core kernels' bounded mbarrier waits: one CTA
+ * allocates tensor memory, waits at most `iterations` polls for a phase that
+ * nothing completes, records the error, releases the tensor memory and
+ * returns; *status = 1 when the wait gave up (the device stays usable). */
+int anacor_wait_guard_check(unsigned iterations, int32_t *status);
 
 /* ---------------------------------------------------------- diagnostics -- */
 

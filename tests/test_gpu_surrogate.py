@@ -16,7 +16,7 @@ import time
 import numpy as np
 import pytest
 
-from anacor_public_gb300 import build, surrogate, synth, tracer
+from anacor_public_gb300 import _lib, build, surrogate, synth, tracer
 from oracle import surrogate_oracle as so
 
 pytestmark = pytest.mark.gpu
@@ -217,6 +217,19 @@ def test_fused_inference_matches_layered_odd_members(members):
     finally:
         model.close()
     assert np.array_equal(e1, e0) and np.array_equal(m1, m0) and np.array_equal(s1, s0)
+
+
+def test_bounded_wait_reports_and_releases():
+    """A tensor-core wait that runs out sets the error word, releases its
+    tensor memory and returns; the next tensor-core work runs normally."""
+    import ctypes as ct
+    L = _lib.load()
+    st = ct.c_int32(-1)
+    assert L.anacor_wait_guard_check(4096, ct.byref(st)) == 0, _lib.last_error(L)
+    assert st.value == 1
+    A = np.ones((128, 64), np.float32)
+    C = surrogate.tc_gemm(A, A)
+    assert np.all(C == 64.0)
 
 
 def test_audited_absorption_small(small, trained_small):

@@ -1,0 +1,48 @@
+"""The surrogate's accuracy bounds on the high-absorption workload.
+
+The 1024x1024x800 mu x5 sample (11.7 M crystal voxels; A_h ~ 0.004-0.01, the
+steepest dependence on direction of any workload).  Training labels are traced
+by the plain kernel on the stride-2 voxel subsample (1.47 M voxels), as the
+bench does; the network is judged against the plain kernel over every voxel on
+2,000 fresh reflections.  Bounds: relative error of the ensemble mean (before
+any audit) median <= 1e-3 and p99 <= 1e-2.
+"""
+import numpy as np
+import pytest
+
+from anacor_public_gb300 import build, surrogate, synth, tracer
+
+pytestmark = pytest.mark.gpu
+
+
+def test_surrogate_bounds_on_the_high_absorption_sample():
+    build.build()
+    s = synth.high_absorption_sample(n_refl=16)
+    sub = s.coords[np.all(s.coords % 2 == 0, axis=1)]
+    model = None
+    plan_t = tracer.Plan(s.label, sub, s.voxel, s.mu)
+    try:
+        omega_t, s1_t, ah_t = surrogate.training_set(s, n=60_000, seed=41, plan=plan_t)
+    finally:
+        plan_t.close()
+    plan = tracer.Plan(s.label, s.coords, s.voxel, s.mu)
+    try:
+        x7_t = surrogate.inputs(omega_t, s1_t, s.xray, s.omega_axis, s.F)
+        model = surrogate.Surrogate(members=4, seed=3, fourier_scale=0.25)
+        model.set_data(x7_t, np.log(ah_t))
+        model.train(10_000, batch=4096, lr_max=3e-3, lr_min=3e-5, total_steps=10_000)
+        omega, s1 = synth.reflections(2000, np.random.default_rng(4040), xray=s.xray)
+        plan.set_reflections(s1, omega, s.xray, s.omega_axis, s.F)
+        plan.configure(12, 0, 1)
+        plan.run()
+        plain = plan.result()
+        mean, spread = model.predict(surrogate.inputs(omega, s1, s.xray, s.omega_axis, s.F))
+    finally:
+        if model is not None:
+            model.close()
+        plan.close()
+    err = surrogate.relative_error(mean, plain)
+    med, p99 = float(np.median(err)), float(np.quantile(err, 0.99))
+    print(f"\n1024x1024x800 mu x5, 2,000 reflections: surrogate vs plain kernel median {med:.2e}, p99 {p99:.2e}, "
+          f"max {err.max():.2e}; {np.mean(spread > 1e-3):.2%} above the spread threshold")
+    assert med <= 1e-3 and p99 <= 1e-2, (med, p99)

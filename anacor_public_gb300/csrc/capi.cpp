@@ -747,10 +747,15 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     // not depend on the device: it runs on a second host thread while this
     // one uploads the volume and voxels and builds the march's fields.
     std::future<int> setup;
-    if (staged && !tables)
-        setup = std::async(std::launch::async, [=] {
-            return setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads);
-        });
+    if (staged && !tables) {
+        try {
+            setup = std::async(std::launch::async, [=] {
+                return setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads);
+            });
+        } catch (...) {
+            // no second thread: the set-up runs on this one below
+        }
+    }
     anacor_plan p;
     int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
     if (!st) {
@@ -760,7 +765,10 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     }
     if (!st && !ib_cls)
         st = plan_default_config(&p);
-    const int setup_st = setup.valid() ? setup.get() : kOk;   // joined on every path
+    // joined on every path (or run here when no second thread was started)
+    const int setup_st = setup.valid() ? setup.get()
+                         : (staged && !tables) ? setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads)
+                                               : kOk;
     if (!st) {
         if (tables)
             std::memcpy(p.h_refl, tables, (size_t)n_refl * sizeof(ReflTable));

@@ -81,7 +81,8 @@ def parse():
                     help="batch: only sample K of the 12 (the same sample as in the full batch)")
     ap.add_argument("--stride-tune", action="store_true",
                     help="batch: choose each sample's voxel stride from {2, 4, 8} by its A_h deviation from "
-                         "stride 1 on 64 reflections (tracer.choose_stride, tolerance 1e-3)")
+                         "stride 1 on 64 reflections (tracer.choose_stride, tolerance 1e-3; under torchrun "
+                         "each rank chooses on its own slice)")
     ap.add_argument("--config", default=None,
                     help="variant,tile,order for a single-sample plan instead of the autotuner (e.g. 8,1024,1)")
     ap.add_argument("--train-refl", type=int, default=100000, help="surrogate: traced training reflections")

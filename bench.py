@@ -12,7 +12,7 @@ path over all reflections.  Other workloads:
            reflections each) in one persistent launch, autotuned and replayed
            from a CUDA graph
   highabs  1024x1024x800 volume, every crystal voxel (~11.7M), mu x5; timed on
-           a reflection subset (--refl, default 256) of the 50,000
+           a reflection subset (--refl, default 2,000) of the 50,000
 
     python bench.py [--workload W] [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -55,7 +55,7 @@ WORKLOADS = {
     "bisection": "1024x1024x800 high-absorption sample, all crystal voxels; iterative-bisection paths "
                  "(ib_test) on a reflection subset, beside the plain march",
 }
-DEFAULT_REFL = {"beamline": 20000, "small": 300, "batch": 0, "highabs": 256, "surrogate": 1000000,
+DEFAULT_REFL = {"beamline": 20000, "small": 300, "batch": 0, "highabs": 2000, "surrogate": 1000000,
                 "highabs_surrogate": 50000, "gridding": 20000, "bisection": 256}
 SURROGATE_METRIC = "reflections/s (surrogate with audit: ensemble A_h, 2% random + high-spread re-traced)"
 

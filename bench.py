@@ -244,6 +244,26 @@ def profiled_traffic(workload: str, key: str = "traffic_bytes_per_launch"):
     return None
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_runner(threads: int):
     """The reference algorithm on the host cores: the reference library where it
     was compiled from its sources, else the oracle port."""
@@ -277,7 +297,7 @@ def cpu_baseline(samples, seconds: float):
     if len(samples) == 1:
         s = samples[0]
         rate, n = cpu_rate(s, seconds, runner)
-        return {"value": rate, "unit": "reflections/s", "cores": threads, "kind": kind,
+        return {"value": rate, "unit": "reflections/s", "cores": threads, "cpu_model": cpu_model(), "kind": kind,
                 "sample": f"first {n} reflections of the workload x {len(s.coords)} voxels (2 rays each)"}
     # a batch: time a slice of every sample and add up the per-sample times
     per = max(0.5, seconds / len(samples))
@@ -287,7 +307,7 @@ def cpu_baseline(samples, seconds: float):
         total_refl += s.n_refl
         total_sec += s.n_refl / rate
         parts.append(n)
-    return {"value": total_refl / total_sec, "unit": "reflections/s", "cores": threads, "kind": kind,
+    return {"value": total_refl / total_sec, "unit": "reflections/s", "cores": threads, "cpu_model": cpu_model(), "kind": kind,
             "sample": f"per sample the first {min(parts)}..{max(parts)} reflections, extrapolated to all "
                       f"{total_refl} reflections of the {len(samples)} samples"}
 
@@ -326,7 +346,7 @@ def run_reference(args):
                    "n_reflections": sum(s.n_refl for s in samples),
                    "step": f"bounded sample: ~{per_step:.0f} s of reflections per step"},
         "voxel_rays_per_s": v * 2 * n_vox / len(samples),
-        "cpu_baseline": {"value": v, "unit": "reflections/s", "cores": threads, "kind": kind,
+        "cpu_baseline": {"value": v, "unit": "reflections/s", "cores": threads, "cpu_model": cpu_model(), "kind": kind,
                          "sample": f"{int(statistics.median(counts))} reflections per sample per step"},
         "e2e": {"value": v, "unit": "reflections/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -72,6 +72,12 @@ struct DeviceState {
 
 std::mutex g_mu;
 DeviceState g_dev[64];
+// The library's stream-ordered memory pool per device.  It keeps up to
+// ANACOR_POOL_KEEP_MB (default 16 GiB) of freed memory between calls, so that
+// a drop-in call does not unmap and map again the gigabyte or so of volume,
+// fields and partial sums it allocates (the default pool returns freed memory
+// at every synchronisation).
+cudaMemPool_t g_pool[64] = {};
 
 // Plan-level variants: 1..4 cooperative march, 5..8 the centred distance
 // field, 9..12 the octant fields, 13..16 the octant fields in 4^3 bricks;
@@ -124,6 +130,21 @@ int current_device(DeviceState **out)
             return fail(kErrCuda, "kernel not loadable on this device");
         if ((e = cudaStreamCreateWithFlags(&d.stream, cudaStreamNonBlocking)) != cudaSuccess)
             return cuda_fail(e, "cudaStreamCreate");
+        {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t pool = nullptr;
+            if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+                const char *mb = std::getenv("ANACOR_POOL_KEEP_MB");
+                uint64_t keep = (uint64_t)(mb ? std::atoll(mb) : 16384) << 20;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+                g_pool[dev] = pool;
+            } else {
+                cudaGetLastError();   // no pool of our own: the device's default pool serves
+            }
+        }
         d.sms = prop.multiProcessorCount;
         d.ready = true;
     }
@@ -137,6 +158,9 @@ cudaError_t dev_alloc(T **p, size_t count, cudaStream_t st)
     *p = nullptr;
     if (count == 0)
         return cudaSuccess;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && g_pool[dev])
+        return cudaMallocFromPoolAsync(reinterpret_cast<void **>(p), count * sizeof(T), g_pool[dev], st);
     return cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T), st);
 }
 

@@ -90,8 +90,10 @@ def test_field_matches_cpu(shape, seed):
     assert np.array_equal(tracer.distance_field(vol), field_cpu(vol))
 
 
-@pytest.mark.parametrize("shape,seed", [((20, 33, 47), 5), ((9, 70, 5), 6), ((1, 1, 90), 7)])
+@pytest.mark.parametrize("shape,seed", [((20, 33, 47), 5), ((9, 70, 5), 6), ((1, 1, 90), 7),
+                                        ((130, 67, 261), 8), ((150, 90, 260), 9), ((3, 140, 132), 10)])
 def test_octant_fields_match_cpu(shape, seed):
+    # several tiles along every axis, rows with and without 4-byte alignment
     vol = blocky_volume(shape, seed)
     assert np.array_equal(tracer.octant_fields(vol), octant_fields_cpu(vol))
 

@@ -4,16 +4,19 @@
 // (reflection_setup.cpp), device buffers, launches and the reference's
 // ownership rules (malloc()ed result freed by the caller's free()).
 #include <cuda_runtime.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
-#include <future>
+#include <condition_variable>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <tuple>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "anacor_gb300.h"
@@ -330,6 +333,95 @@ ReflTable *thread_staging(int64_t n_refl)
     }
     return s.p;
 }
+
+// A helper thread per calling thread, kept between calls, for the
+// reflections' host set-up while the caller drives the device.  The OpenMP
+// team the set-up opens belongs to the helper and is reused by the next call
+// (a new thread per call opened a new team each time: about a millisecond,
+// as long as the whole device work of a few hundred reflections).
+class SetupHelper {
+public:
+    ~SetupHelper()
+    {
+        if (!owned())
+            return;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            quit_ = true;
+        }
+        cv_.notify_all();
+        if (th_.joinable())
+            th_.join();
+    }
+    // false when no helper thread can be started (the caller runs f itself)
+    bool submit(std::function<int()> f)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        owned();
+        if (!th_.joinable()) {
+            try {
+                th_ = std::thread([this] { loop(); });
+                pid_ = getpid();
+            } catch (...) {
+                return false;
+            }
+        }
+        job_ = std::move(f);
+        pending_ = true;
+        finished_ = false;
+        cv_.notify_all();
+        return true;
+    }
+    int wait()
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [this] { return finished_; });
+        finished_ = false;
+        return result_;
+    }
+
+private:
+    // After fork() a child inherits the handle of a helper that runs only in
+    // the parent: the handle is given up (never joined) and a new helper is
+    // started on the child's first call.
+    bool owned()
+    {
+        if (th_.joinable() && pid_ != getpid()) {
+            new std::thread(std::move(th_));   // left to the parent's process
+            return false;
+        }
+        return true;
+    }
+    void loop()
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [this] { return pending_ || quit_; });
+            if (!pending_)
+                return;
+            std::function<int()> f = std::move(job_);
+            pending_ = false;
+            lk.unlock();
+            int r;
+            try {
+                r = f();
+            } catch (...) {
+                r = kErrNoMem;
+            }
+            lk.lock();
+            result_ = r;
+            finished_ = true;
+            cv_.notify_all();
+        }
+    }
+    std::thread th_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::function<int()> job_;
+    bool pending_ = false, finished_ = false, quit_ = false;
+    int result_ = kOk;
+    pid_t pid_ = 0;
+};
 
 // the tile actually used: at least `tile`, and large enough that a reflection
 // has at most kMaxTilesPerRefl tiles (a multiple of 32 voxels)
@@ -768,18 +860,12 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     // allocation per call); the plan lives for this call only
     ReflTable *staged = n_refl > 0 ? thread_staging(n_refl) : nullptr;
     // The reflections' host set-up (FP64 rotation, angles, face rules) does
-    // not depend on the device: it runs on a second host thread while this
+    // not depend on the device: it runs on this thread's helper while this
     // one uploads the volume and voxels and builds the march's fields.
-    std::future<int> setup;
-    if (staged && !tables) {
-        try {
-            setup = std::async(std::launch::async, [=] {
-                return setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads);
-            });
-        } catch (...) {
-            // no second thread: the set-up runs on this one below
-        }
-    }
+    static thread_local SetupHelper helper;
+    const bool on_helper = staged && !tables && helper.submit([=] {
+        return setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads);
+    });
     anacor_plan p;
     int st = plan_init(&p, flat, shape, coords, n, voxel, mu, full, is_exp);
     if (!st) {
@@ -790,7 +876,7 @@ int run_once(const int8_t *flat, const int64_t *shape, const int64_t *coords, in
     if (!st && !ib_cls)
         st = plan_default_config(&p);
     // joined on every path (or run here when no second thread was started)
-    const int setup_st = setup.valid() ? setup.get()
+    const int setup_st = on_helper ? helper.wait()
                          : (staged && !tables) ? setup_reflections(axis, omega, F, xray, s1, n_refl, staged, threads)
                                                : kOk;
     if (!st) {

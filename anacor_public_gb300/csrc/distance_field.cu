@@ -116,35 +116,52 @@ constexpr int kRowThreads = 256;
 constexpr int kRowChunk = 4 * kRowThreads;   // 4 voxels per thread
 constexpr int kRowWords = kRowChunk / 32 + 2;
 
-__global__ void __launch_bounds__(kRowThreads) octant_rows(const int8_t *__restrict__ vol, int dx, long long nvol,
-                                                           bool vec, uint8_t *__restrict__ out, int *__restrict__ bad)
+// (volumes hold fewer than 2^31 voxels: 32-bit positions)
+__global__ void __launch_bounds__(kRowThreads) octant_rows(const int8_t *__restrict__ vol, int dx, int nvol, bool vec,
+                                                           uint8_t *__restrict__ out, int *__restrict__ bad)
 {
-    __shared__ uint32_t change[kRowWords];   // word k covers p0 + 32 (k - 1) ...
-    const long long p0 = (long long)blockIdx.x * kRowChunk;
+    __shared__ uint32_t change[kRowWords];          // word k covers p0 + 32 (k - 1) ...
+    __shared__ uint32_t labw[kRowChunk / 4 + 17];   // bytes p0 - 32 ... p0 + kRowChunk + 35
+    const int p0 = blockIdx.x * kRowChunk;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint8_t *lb = reinterpret_cast<uint8_t *>(labw);
+    // the chunk's labels (a word per thread) and 32 / 36 bytes either side
+    {
+        const int v = p0 + 4 * (int)threadIdx.x;
+        uint32_t w = 0;
+        if (vec && v + 3 < nvol)
+            w = __ldg(reinterpret_cast<const uint32_t *>(vol + v));
+        else
+            for (int k = 0; k < 4; k++)
+                if (v + k < nvol)
+                    w |= (uint32_t)(uint8_t)vol[v + k] << (8 * k);
+        labw[8 + threadIdx.x] = w;
+        if (threadIdx.x < 68) {
+            const int h = threadIdx.x < 32 ? (int)threadIdx.x : kRowChunk + 32 + (int)threadIdx.x - 32;
+            const int q = p0 - 32 + h;
+            lb[h] = (q >= 0 && q < nvol) ? (uint8_t)vol[q] : 0u;
+        }
+    }
+    __syncthreads();
+    const int x0 = p0 % dx;   // x of p0; x of p0 + o is (x0 + o) mod dx
     for (int k = warp; k < kRowWords; k += kRowThreads / 32) {
-        const long long p = p0 + 32ll * (k - 1) + lane;
+        const int o = 32 * (k - 1) + lane;   // offset from p0, -32 ... kRowChunk + 31
+        const int p = p0 + o;
         bool b = false;
-        if (p >= 0 && p + 1 < nvol && (p + 1) % dx != 0)
-            b = vol[p] != vol[p + 1];
+        if (p >= 0 && p + 1 < nvol && (x0 + o + 1 + dx) % dx != 0)
+            b = lb[o + 32] != lb[o + 33];
         const uint32_t m = __ballot_sync(0xffffffffu, b);
         if (lane == 0)
             change[k] = m;
     }
     __syncthreads();
-    const long long v0 = p0 + 4 * threadIdx.x;
+    const int v0 = p0 + 4 * (int)threadIdx.x;
     if (v0 >= nvol)
         return;
-    uint32_t labs;
-    if (vec && v0 + 3 < nvol) {
-        labs = __ldg(reinterpret_cast<const uint32_t *>(vol + v0));
-    } else {
-        labs = 0;
-        for (int k = 0; k < 4 && v0 + k < nvol; k++)
-            labs |= (uint32_t)(uint8_t)vol[v0 + k] << (8 * k);
-    }
+    const uint32_t labs = labw[8 + threadIdx.x];
     bool any_bad = false;
     uint32_t o0 = 0, o1 = 0;
+    const int xb = (x0 + 4 * (int)threadIdx.x) % dx;   // x of v0
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const int lab = (int)(int8_t)(labs >> (8 * k));
@@ -154,20 +171,23 @@ __global__ void __launch_bounds__(kRowThreads) octant_rows(const int8_t *__restr
         }
         if (lab == 0)
             continue;
-        const int q = 4 * threadIdx.x + k + 32;   // bit index in change[]
+        const int q = 4 * (int)threadIdx.x + k + 32;   // bit index in change[]
         const int w = q >> 5, bit = q & 31;
-        const long long v = v0 + k;
-        const long long rs = v - v % dx, re = rs + dx;   // v's row [rs, re)
+        const int v = v0 + k;
+        int x = xb + k;
+        while (x >= dx)   // at most 3 times
+            x -= dx;
+        const int rs = v - x, re = rs + dx;   // v's row [rs, re)
         int d0 = kFieldCap, d1 = kFieldCap;
         // toward +x: the first change at or after v ends the run at it
         uint32_t m = change[w] >> bit;
-        long long b = -1;
+        int b = -1;
         if (m)
             b = v + __ffs(m) - 1;
         else if ((m = change[w + 1]) != 0)
             b = v + 32 - bit + __ffs(m) - 1;
         if (b >= 0 && b < re)
-            d0 = (int)min(b + 1 - v, (long long)kFieldCap);
+            d0 = min(b + 1 - v, kFieldCap);
         // toward -x: the last change before v, at b, leaves v - b voxels
         m = bit ? change[w] & ((1u << bit) - 1u) : 0u;
         b = -1;
@@ -176,17 +196,17 @@ __global__ void __launch_bounds__(kRowThreads) octant_rows(const int8_t *__restr
         else if ((m = change[w - 1]) != 0)
             b = v - bit - 32 + (31 - __clz(m));
         if (b >= rs)
-            d1 = (int)min(v - b, (long long)kFieldCap);
+            d1 = min(v - b, kFieldCap);
         o0 |= (uint32_t)(lab | (d0 << 3)) << (8 * k);
         o1 |= (uint32_t)(lab | (d1 << 3)) << (8 * k);
     }
     if (vec && v0 + 3 < nvol) {
         *reinterpret_cast<uint32_t *>(out + v0) = o0;
-        *reinterpret_cast<uint32_t *>(out + nvol + v0) = o1;
+        *reinterpret_cast<uint32_t *>(out + (long long)nvol + v0) = o1;
     } else {
         for (int k = 0; k < 4 && v0 + k < nvol; k++) {
             out[v0 + k] = (uint8_t)(o0 >> (8 * k));
-            out[nvol + v0 + k] = (uint8_t)(o1 >> (8 * k));
+            out[(long long)nvol + v0 + k] = (uint8_t)(o1 >> (8 * k));
         }
     }
     if (any_bad)
@@ -396,8 +416,8 @@ cudaError_t launch_octant_fields(const int8_t *d_vol, const int *dims, uint8_t *
     const bool vec = dims[2] % 4 == 0 && ((uintptr_t)d_tmp & 3u) == 0 && ((uintptr_t)d_out & 3u) == 0;
     const unsigned xt = (unsigned)(dims[2] + kLiftWords * 4 - 1) / (kLiftWords * 4);
     const bool vrow = nvol % 4 == 0 && ((uintptr_t)d_vol & 3u) == 0 && ((uintptr_t)d_tmp & 3u) == 0;
-    octant_rows<<<(unsigned)((nvol + kRowChunk - 1) / kRowChunk), kRowThreads, 0, st>>>(d_vol, dims[2], nvol, vrow,
-                                                                                       d_tmp, d_bad);
+    octant_rows<<<(unsigned)((nvol + kRowChunk - 1) / kRowChunk), kRowThreads, 0, st>>>(d_vol, dims[2], (int)nvol,
+                                                                                       vrow, d_tmp, d_bad);
     const dim3 gy(xt, (unsigned)dims[0], (unsigned)(dims[1] + kLiftRows - 1) / kLiftRows);
     octant_lift<2, false><<<gy, kLiftThreads, kLiftSmem, st>>>(d_tmp, dims[1], dims[2], plane, dims[2], nvol, vec,
                                                                d_tmp + 2 * nvol);

@@ -254,6 +254,45 @@ def test_dropin_ray_tracing_overall_like_anacor_worker(lib, small, golden_dir):
     assert max_rel(corr, gold) <= RTOL
 
 
+def test_dropin_calls_from_several_host_threads(lib, small, golden_dir):
+    """Concurrent calls (each host thread has its own pinned staging and
+    set-up helper; the device stream and tuning cache are shared) return the
+    answers of one call, bit for bit, every time."""
+    import threading
+    tab, keep = row_table(small.label)
+    n = small.n_refl
+
+    def call():
+        res = lib.ray_tracing_overall(0, n, small.coords, len(small.coords), small.s1, small.omega, small.xray,
+                                      small.omega_axis, small.F, n, small.voxel, small.mu, tab, small.shape, 0, 0,
+                                      4, 1)
+        assert res, lib.anacor_last_error()
+        out = np.array([res[i] for i in range(n)])
+        lib.free(ct.cast(res, ct.c_void_p))
+        return out
+
+    want = call()
+    got, errors = [], []
+
+    def worker():
+        try:
+            for _ in range(4):
+                got.append(call())
+        except Exception as ex:   # reported below
+            errors.append(ex)
+
+    threads = [threading.Thread(target=worker) for _ in range(3)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not any(t.is_alive() for t in threads)
+    assert not errors, errors
+    assert len(got) == 12
+    for g in got:
+        assert np.array_equal(g, want)
+
+
 def test_dropin_non_contiguous_row_table(lib, small, oracle):
     # rows of the table scattered in memory: the library gathers them
     s = small.subset(refl=slice(0, 5))

@@ -155,16 +155,25 @@ int current_device(DeviceState **out)
     return kOk;
 }
 
+}  // namespace
+
+cudaError_t anacor::lib_malloc_async(void **p, size_t bytes, cudaStream_t st)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && g_pool[dev])
+        return cudaMallocFromPoolAsync(p, bytes, g_pool[dev], st);
+    return cudaMallocAsync(p, bytes, st);
+}
+
+namespace {
+
 template <class T>
 cudaError_t dev_alloc(T **p, size_t count, cudaStream_t st)
 {
     *p = nullptr;
     if (count == 0)
         return cudaSuccess;
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && g_pool[dev])
-        return cudaMallocFromPoolAsync(reinterpret_cast<void **>(p), count * sizeof(T), g_pool[dev], st);
-    return cudaMallocAsync(reinterpret_cast<void **>(p), count * sizeof(T), st);
+    return lib_malloc_async(reinterpret_cast<void **>(p), count * sizeof(T), st);
 }
 
 template <class T>

@@ -75,7 +75,7 @@ cudaError_t count_sampled_voxels(const int8_t *d_vol, const int *dims, int code,
     void *tmp = nullptr;
     cudaError_t e = cub::DeviceReduce::Sum(nullptr, tmp_bytes, flags, d_count, (int)n, st);
     if (!e)
-        e = cudaMallocAsync(&tmp, tmp_bytes, st);
+        e = lib_malloc_async(reinterpret_cast<void **>(&tmp), tmp_bytes, st);
     if (!e)
         e = cub::DeviceReduce::Sum(tmp, tmp_bytes, flags, d_count, (int)n, st);
     if (tmp)
@@ -93,7 +93,7 @@ cudaError_t select_sampled_voxels(const int8_t *d_vol, const int *dims, int code
     void *tmp = nullptr;
     cudaError_t e = cub::DeviceSelect::If(nullptr, tmp_bytes, idx, d_lin, d_count, (int)n, p, st);
     if (!e)
-        e = cudaMallocAsync(&tmp, tmp_bytes, st);
+        e = lib_malloc_async(reinterpret_cast<void **>(&tmp), tmp_bytes, st);
     if (!e)
         e = cub::DeviceSelect::If(tmp, tmp_bytes, idx, d_lin, d_count, (int)n, p, st);
     if (tmp)

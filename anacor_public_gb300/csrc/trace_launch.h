@@ -103,6 +103,9 @@ int plan_view(const anacor_plan *p, PlanView *out);
 int plan_view_field(anacor_plan *p, PlanView *out);
 
 int rcp_table_init();
+// Stream-ordered allocation from the library's pool of the current device
+// (the device's default pool when it has none); freed with cudaFreeAsync.
+cudaError_t lib_malloc_async(void **p, size_t bytes, cudaStream_t st);
 int absorption_block_threads();
 // Launch the absorption kernel over no work with `threads` (a multiple of 32,
 // at most the kernel's block size) threads per block; *status_out is the

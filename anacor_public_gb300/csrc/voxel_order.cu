@@ -109,9 +109,9 @@ cudaError_t launch_order_permutation(const long long *d_c, int n, const int *dim
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
     cudaError_t e;
-    if ((e = cudaMallocAsync(&keys, 2 * sizeof(unsigned long long) * (size_t)n, st)))
+    if ((e = lib_malloc_async(reinterpret_cast<void **>(&keys), 2 * sizeof(unsigned long long) * (size_t)n, st)))
         return e;
-    if ((e = cudaMallocAsync(&idx, sizeof(int) * (size_t)n, st))) {
+    if ((e = lib_malloc_async(reinterpret_cast<void **>(&idx), sizeof(int) * (size_t)n, st))) {
         cudaFreeAsync(keys, st);
         return e;
     }
@@ -122,7 +122,7 @@ cudaError_t launch_order_permutation(const long long *d_c, int n, const int *dim
     if (!e)
         e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys + n, idx, d_perm, n, 0, bits, st);
     if (!e)
-        e = cudaMallocAsync(&tmp, tmp_bytes, st);
+        e = lib_malloc_async(reinterpret_cast<void **>(&tmp), tmp_bytes, st);
     if (!e)
         e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys + n, idx, d_perm, n, 0, bits, st);
     if (tmp)
@@ -145,9 +145,9 @@ cudaError_t launch_pack_coords_order(const long long *d_c, int n, const int *dim
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
     cudaError_t e;
-    if ((e = cudaMallocAsync(&keys, 2 * sizeof(unsigned long long) * (size_t)n, st)))
+    if ((e = lib_malloc_async(reinterpret_cast<void **>(&keys), 2 * sizeof(unsigned long long) * (size_t)n, st)))
         return e;
-    if ((e = cudaMallocAsync(&vals, sizeof(unsigned long long) * (size_t)n, st))) {
+    if ((e = lib_malloc_async(reinterpret_cast<void **>(&vals), sizeof(unsigned long long) * (size_t)n, st))) {
         cudaFreeAsync(keys, st);
         return e;
     }
@@ -162,7 +162,7 @@ cudaError_t launch_pack_coords_order(const long long *d_c, int n, const int *dim
     if (!e)
         e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys, keys2, vals, out, n, 0, bits, st);
     if (!e)
-        e = cudaMallocAsync(&tmp, tmp_bytes, st);
+        e = lib_malloc_async(reinterpret_cast<void **>(&tmp), tmp_bytes, st);
     if (!e)
         e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, keys, keys2, vals, out, n, 0, bits, st);
     if (tmp)

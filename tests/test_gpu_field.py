@@ -91,7 +91,8 @@ def test_field_matches_cpu(shape, seed):
 
 
 @pytest.mark.parametrize("shape,seed", [((20, 33, 47), 5), ((9, 70, 5), 6), ((1, 1, 90), 7),
-                                        ((130, 67, 261), 8), ((150, 90, 260), 9), ((3, 140, 132), 10)])
+                                        ((130, 67, 261), 8), ((150, 90, 260), 9), ((3, 140, 132), 10),
+                                        ((40, 50, 1), 11), ((1, 200, 3), 12), ((70, 1, 70), 13)])
 def test_octant_fields_match_cpu(shape, seed):
     # several tiles along every axis, rows with and without 4-byte alignment
     vol = blocky_volume(shape, seed)

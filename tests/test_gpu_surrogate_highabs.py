@@ -3,7 +3,7 @@
 The 1024x1024x800 mu x5 sample (11.7 M crystal voxels; A_h ~ 0.004-0.01, the
 steepest dependence on direction of any workload).  Training labels are traced
 by the plain kernel on the stride-2 voxel subsample (1.47 M voxels), as the
-bench does; the network is judged against the plain kernel over every voxel on
+bench does; the network is compared with the plain kernel over every voxel on
 2,000 fresh reflections.  Bounds: relative error of the ensemble mean (before
 any audit) median <= 1e-3 and p99 <= 1e-2.
 """

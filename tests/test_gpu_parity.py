@@ -293,6 +293,24 @@ def test_dropin_calls_from_several_host_threads(lib, small, golden_dir):
         assert np.array_equal(g, want)
 
 
+def test_dropin_calls_keep_device_memory_steady(lib, small):
+    """Repeated calls reuse the library pool's memory: after the first call
+    the device's free memory does not move (no leak, no growing reservation)."""
+    import torch
+    tab, keep = row_table(small.label)
+    n = small.n_refl
+    free = []
+    for _ in range(4):
+        res = lib.ray_tracing_overall(0, n, small.coords, len(small.coords), small.s1, small.omega, small.xray,
+                                      small.omega_axis, small.F, n, small.voxel, small.mu, tab, small.shape, 0, 0,
+                                      4, 1)
+        assert res, lib.anacor_last_error()
+        lib.free(ct.cast(res, ct.c_void_p))
+        torch.cuda.synchronize()
+        free.append(torch.cuda.mem_get_info()[0])
+    assert free[1] == free[2] == free[3], free
+
+
 def test_dropin_non_contiguous_row_table(lib, small, oracle):
     # rows of the table scattered in memory: the library gathers them
     s = small.subset(refl=slice(0, 5))

@@ -83,7 +83,36 @@ void my_frame(const double *v, double *out)
 // Signed step ratios per exit face.  The reference writes each face as
 // "new = R(c +/- i * ratio)"; "c - fl(i*r)" is the IEEE operation
 // "c + fl(i*(-r))", so the sign is folded into q.  Axis order (z, y, x).
-void face_rule(int face, double th, double ph, FaceRule &r)
+// The libm values the six face rules of one leg use, each evaluated once
+// (several rules share them; every rule reads the same expressions as its
+// reference formula, so the ratios are bit for bit those of separate calls).
+struct LegTrig {
+    double tan_th, tan_pi_th, tan_ph, cos_ph, tan_aph, sin_aph, cos_aph, sin_ph;
+    double tan_ath, tan_pi_ath, sin_mph;   // by the |theta| < pi/2 branch
+};
+
+void leg_trig(double th, double ph, LegTrig &t)
+{
+    const double half = kPi / 2;
+    t.tan_th = std::tan(th);
+    t.tan_pi_th = std::tan(kPi - th);
+    t.tan_ph = std::tan(ph);
+    t.cos_ph = std::cos(ph);
+    t.tan_aph = std::tan(std::fabs(ph));
+    t.sin_aph = std::sin(std::fabs(ph));
+    t.cos_aph = std::cos(std::fabs(ph));
+    t.sin_ph = std::sin(ph);
+    if (std::fabs(th) < half) {
+        t.tan_ath = std::tan(std::fabs(th));
+        t.tan_pi_ath = t.sin_mph = 0.0;
+    } else {
+        t.tan_ath = 0.0;
+        t.tan_pi_ath = std::tan(kPi - std::fabs(th));
+        t.sin_mph = std::sin(-ph);
+    }
+}
+
+void face_rule(int face, double th, double ph, const LegTrig &t, FaceRule &r)
 {
     const double half = kPi / 2;
     const bool lower = th > 0;   // floor when theta > 0, else round (faces 6, 2, 3, 1)
@@ -94,19 +123,19 @@ void face_rule(int face, double th, double ph, FaceRule &r)
     case 6:   // x_min, ray_tracing_basic.c:418-509
         r.status = std::fabs(th) <= half ? kOk : kErrAssert;
         r.q[2] = -1;
-        r.q[1] = -(std::tan(th) / std::cos(ph));
-        r.q[0] = std::tan(ph);
+        r.q[1] = -(t.tan_th / t.cos_ph);
+        r.q[0] = t.tan_ph;
         r.count_axis = 2; r.count_kind = 0;
         break;
     case 2:   // z_min, :512-709
         if (std::fabs(th) < half) {
             r.status = ph < 0 ? kOk : kErrAssert;
-            r.q[2] = -(1 / std::tan(std::fabs(ph)));
-            r.q[1] = -(std::tan(th) / std::sin(std::fabs(ph)));
+            r.q[2] = -(1 / t.tan_aph);
+            r.q[1] = -(t.tan_th / t.sin_aph);
         } else {
             r.status = ph > 0 ? kOk : kErrAssert;
-            r.q[2] = 1 / std::tan(std::fabs(ph));
-            r.q[1] = -(std::tan(kPi - th) / std::sin(std::fabs(ph)));
+            r.q[2] = 1 / t.tan_aph;
+            r.q[1] = -(t.tan_pi_th / t.sin_aph);
         }
         r.q[0] = -1;
         r.count_axis = 0; r.count_kind = 0;
@@ -114,13 +143,13 @@ void face_rule(int face, double th, double ph, FaceRule &r)
     case 3:   // z_max, :712-896
         if (std::fabs(th) < half) {
             r.status = ph > 0 ? kOk : kErrAssert;
-            r.q[2] = -(1 / std::tan(std::fabs(ph)));
-            r.q[1] = -(std::tan(th) / std::sin(std::fabs(ph)));
+            r.q[2] = -(1 / t.tan_aph);
+            r.q[1] = -(t.tan_th / t.sin_aph);
             r.count_kind = 1;
         } else {
             r.status = ph < 0 ? kOk : kErrAssert;
-            r.q[2] = 1 / (std::tan(std::fabs(ph)));
-            r.q[1] = -(std::tan(kPi - th) / std::sin(std::fabs(ph)));
+            r.q[2] = 1 / t.tan_aph;
+            r.q[1] = -(t.tan_pi_th / t.sin_aph);
             r.count_kind = 2;
         }
         r.q[0] = 1;
@@ -129,11 +158,11 @@ void face_rule(int face, double th, double ph, FaceRule &r)
     case 4:   // y_min, :899-1101; always floor
         r.status = th > 0 ? kOk : kErrAssert;
         if (std::fabs(th) < half) {
-            r.q[2] = -(std::cos(std::fabs(ph)) / std::tan(std::fabs(th)));
-            r.q[0] = std::sin(ph) / std::tan(std::fabs(th));
+            r.q[2] = -(t.cos_aph / t.tan_ath);
+            r.q[0] = t.sin_ph / t.tan_ath;
         } else {
-            r.q[2] = std::cos(std::fabs(ph)) / (std::tan((kPi - std::fabs(th))));
-            r.q[0] = std::sin(-ph) / (std::tan((kPi - std::fabs(th))));
+            r.q[2] = t.cos_aph / t.tan_pi_ath;
+            r.q[0] = t.sin_mph / t.tan_pi_ath;
         }
         r.q[1] = -1;
         r.use_round = 0;
@@ -142,12 +171,12 @@ void face_rule(int face, double th, double ph, FaceRule &r)
     case 5:   // y_max, :1104-1277; always round
         r.status = th < 0 ? kOk : kErrAssert;
         if (std::fabs(th) < half) {
-            r.q[2] = -(std::cos(std::fabs(ph)) / (std::tan(std::fabs(th))));
-            r.q[0] = std::sin(ph) / (std::tan(std::fabs(th)));
+            r.q[2] = -(t.cos_aph / t.tan_ath);
+            r.q[0] = t.sin_ph / t.tan_ath;
             r.count_kind = 1;
         } else {
-            r.q[2] = std::cos(std::fabs(ph)) / (std::tan(kPi - std::fabs(th)));
-            r.q[0] = -(std::sin(ph) / (std::tan(kPi - std::fabs(th))));
+            r.q[2] = t.cos_aph / t.tan_pi_ath;
+            r.q[0] = -(t.sin_ph / t.tan_pi_ath);
             r.count_kind = 2;
         }
         r.q[1] = 1;
@@ -157,8 +186,8 @@ void face_rule(int face, double th, double ph, FaceRule &r)
     default:  // 1, x_max, :1280-1372
         r.status = std::fabs(th) >= half ? kOk : kErrAssert;
         r.q[2] = 1;
-        r.q[1] = -(std::tan(kPi - th) / std::cos(std::fabs(ph)));
-        r.q[0] = -(std::tan(ph));
+        r.q[1] = -(t.tan_pi_th / t.cos_aph);
+        r.q[0] = -(t.tan_ph);
         r.count_axis = 2; r.count_kind = 1;
         r.vac_limit = 10;
         break;
@@ -213,9 +242,11 @@ int fill_leg(const double *dir_my, bool incident, double th, double ph, LegHead 
     }
     if (!nonzero)
         return kErrDirection;
+    LegTrig t;
+    leg_trig(th, ph, t);
     for (int f = 1; f <= 6; f++) {
         std::memset(&rules[f - 1], 0, sizeof(FaceRule));
-        face_rule(f, th, ph, rules[f - 1]);
+        face_rule(f, th, ph, t, rules[f - 1]);
     }
     return kOk;
 }

@@ -254,18 +254,25 @@ def test_dropin_ray_tracing_overall_like_anacor_worker(lib, small, golden_dir):
     assert max_rel(corr, gold) <= RTOL
 
 
-def test_dropin_calls_from_several_host_threads(lib, small, golden_dir):
+@pytest.fixture(scope="module")
+def beamline_500():
+    return synth.beamline_sample().subset(refl=slice(0, 500))
+
+
+@pytest.mark.parametrize("which", ["small", "beamline_500"])
+def test_dropin_calls_from_several_host_threads(lib, which, request):
     """Concurrent calls (each host thread has its own pinned staging and
-    set-up helper; the device stream and tuning cache are shared) return the
-    answers of one call, bit for bit, every time."""
+    set-up helper; the device stream and tuning cache are shared; a 105 MB
+    pageable volume is page-locked for its upload, one call at a time) return
+    the answers of one call, bit for bit, every time."""
     import threading
-    tab, keep = row_table(small.label)
-    n = small.n_refl
+    smp = request.getfixturevalue(which)
+    tab, keep = row_table(smp.label)
+    n = smp.n_refl
 
     def call():
-        res = lib.ray_tracing_overall(0, n, small.coords, len(small.coords), small.s1, small.omega, small.xray,
-                                      small.omega_axis, small.F, n, small.voxel, small.mu, tab, small.shape, 0, 0,
-                                      4, 1)
+        res = lib.ray_tracing_overall(0, n, smp.coords, len(smp.coords), smp.s1, smp.omega, smp.xray,
+                                      smp.omega_axis, smp.F, n, smp.voxel, smp.mu, tab, smp.shape, 0, 0, 4, 1)
         assert res, lib.anacor_last_error()
         out = np.array([res[i] for i in range(n)])
         lib.free(ct.cast(res, ct.c_void_p))

@@ -1231,21 +1231,50 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) absorption_kernel(const Sa
 // down to the resolution 1.0; boundary 0: a label equal to cls moves longest
 // in, boundary 1: it moves shortest out.  The point is floor(c + floor(mid) q).
 // A position outside the volume (undefined in the reference) fails the ray.
-__device__ __forceinline__ bool bisect_dev(double longest, double shortest, int cz, int cy, int cx, const double *q,
-                                           const Vol &v, int boundary, int cls, int *p, double &mid)
+//
+// The probe points floor(c + fl(mid * q)) come from fixed point where that is
+// exact: mid in 24.40 (truncated) times the rule's Q = llrint(q * 2^32) is a
+// 128-bit product read as 56.72; its error is below 1.1e-6 for |q| < 2^16 and
+// |mid q| < 2^14 (every point inside the volume), and the FP64 expression's
+// own rounding below 1e-11, so a fraction more than 2^-18 from an integer has
+// the reference's floor.  Nearer than that (or a rule without Q) the FP64
+// expression is evaluated; the range tests sit on integers and are covered by
+// the same margin.  The FP64 pipe, which binds this kernel, keeps only the
+// bisection of [shortest, longest] itself.
+__device__ __forceinline__ bool bisect_dev(double longest, double shortest, int cz, int cy, int cx,
+                                           const FaceRule &R, const Vol &v, int boundary, int cls, int *p,
+                                           double &mid)
 {
+    const double *q = R.q;
     const double c[3] = {(double)cz, (double)cy, (double)cx};
+    const int ci[3] = {cz, cy, cx};
     const int dim[3] = {v.dz, v.dy, v.dx};
+    constexpr unsigned long long kMargin = 1ull << 46;   // 2^-18 of the 64-bit fraction
     double diff = __dadd_rn(longest, -shortest);
     mid = __dmul_rn(__dadd_rn(longest, shortest), 0.5);
     while (diff > 1.0) {
         mid = __dmul_rn(__dadd_rn(longest, shortest), 0.5);
+        const long long mfx = R.fast ? __double2ll_rz(__dmul_rn(mid, 1099511627776.0)) : 0ll;   // mid * 2^40
         int pp[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            const double x = floor(__dadd_rn(c[a], __dmul_rn(mid, q[a])));
-            if (!(x >= 0.0 && x < (double)dim[a]))
+            bool exact = !R.fast;
+            long long x = 0;
+            if (!exact) {
+                const long long hi = __mul64hi(mfx, R.Q[a]);
+                const unsigned long long lo = (unsigned long long)mfx * (unsigned long long)R.Q[a];
+                const unsigned long long frac = ((unsigned long long)(hi & 0xff) << 56) | (lo >> 8);
+                exact = frac < kMargin || frac > ~kMargin;
+                x = (long long)ci[a] + (hi >> 8);
+            }
+            if (exact) {
+                const double xd = floor(__dadd_rn(c[a], __dmul_rn(mid, q[a])));
+                if (!(xd >= 0.0 && xd < (double)dim[a]))
+                    return false;
+                x = (long long)xd;
+            } else if (x < 0 || x >= dim[a]) {
                 return false;
+            }
             pp[a] = (int)x;
         }
         const int lab = __ldg(v.p + ((long long)pp[0] * v.dy + pp[1]) * v.dx + pp[2]);
@@ -1302,16 +1331,16 @@ __device__ __noinline__ int ib_leg(const LegHead &h, const FaceRule *rules, int 
     const int p0[3] = {cz, cy, cx};
     int air[3], cr[3], li[3], lo[3], bi[3], bo[3];
     double m_air, m_cr, m_li, m_lo, m_bi, m_bo;
-    if (!bisect_dev(air_longest, 0.0, cz, cy, cx, R.q, v, 0, 0, air, m_air) ||
-        !bisect_dev(m_air, 0.0, cz, cy, cx, R.q, v, 1, 3, cr, m_cr))
+    if (!bisect_dev(air_longest, 0.0, cz, cy, cx, R, v, 0, 0, air, m_air) ||
+        !bisect_dev(m_air, 0.0, cz, cy, cx, R, v, 1, 3, cr, m_cr))
         return kErrArgs;
     int npts = 3;
     const int *pa = nullptr, *pb = nullptr, *pc = nullptr, *pd = nullptr;   // points 3..6
     do {
-        if (!bisect_dev(m_air, m_cr, cz, cy, cx, R.q, v, 0, 2, li, m_li))
+        if (!bisect_dev(m_air, m_cr, cz, cy, cx, R, v, 0, 2, li, m_li))
             return kErrArgs;
         if (__ddiv_rn(abs_sum3(li, air), 3.0) > 1.0) {
-            if (!bisect_dev(m_air, m_li, cz, cy, cx, R.q, v, 1, 2, lo, m_lo))
+            if (!bisect_dev(m_air, m_li, cz, cy, cx, R, v, 1, 2, lo, m_lo))
                 return kErrArgs;
             if (__ddiv_rn(abs_sum3(li, lo), 3.0) <= 2.0)
                 break;
@@ -1320,10 +1349,10 @@ __device__ __noinline__ int ib_leg(const LegHead &h, const FaceRule *rules, int 
             npts = 5;
         }
         if (num_cls > 3) {
-            if (!bisect_dev(m_air, m_cr, cz, cy, cx, R.q, v, 0, 4, bi, m_bi))
+            if (!bisect_dev(m_air, m_cr, cz, cy, cx, R, v, 0, 4, bi, m_bi))
                 return kErrArgs;
             if (abs_sum3(bi, air) > 1.0) {
-                if (!bisect_dev(m_air, m_bi, cz, cy, cx, R.q, v, 1, 4, bo, m_bo))
+                if (!bisect_dev(m_air, m_bi, cz, cy, cx, R, v, 1, 4, bo, m_bo))
                     return kErrArgs;
                 if (__ddiv_rn(abs_sum3(bi, bo), 3.0) <= 2.0)
                     break;
